@@ -55,6 +55,7 @@ class RefCase(C.Structure):
         ("bry", _dp), ("qq", _dp), ("nqq", C.c_int), ("dtoq", C.c_double),
         ("xcoor_c", C.c_double), ("ycoor_c", C.c_double), ("mask", _ip), ("lkout", C.c_int),
         ("efdc_basetime", C.c_double), ("max_samples", C.c_int), ("nthreads", C.c_int),
+        ("warm_iters", C.c_int),
     ]
 
 
@@ -63,6 +64,7 @@ class RefOut(C.Structure):
         ("h", _dp), ("um", _dp), ("vn", _dp), ("uu", _dp), ("vv", _dp), ("uua", _dp),
         ("vva", _dp), ("iters", C.c_longlong), ("time", C.c_double), ("water_cells", C.c_int),
         ("nqs", C.c_int), ("nsamples", C.c_int), ("bc", _ip), ("val", _dp),
+        ("loop_seconds", C.c_double),
     ]
 
 
@@ -282,7 +284,7 @@ def couple_values(rows, cols, dx, dy, side, cell, h, uua, vva):
 
 def run_reference(case: Case, nthreads: int = 1, mask=None, lkout: int = 0,
                   efdc_basetime: float = 3600.0, max_samples: int = 0, evap_inputs=None,
-                  sources=None):
+                  sources=None, warm_iters: int = 0, want_fields: bool = True):
     """Run the reference's own kernels (CPU build) on a case in fixed-dt mode.
 
     Returns the reference-layout fields reshaped to (rows, cols) plus the raw
@@ -326,7 +328,8 @@ def run_reference(case: Case, nthreads: int = 1, mask=None, lkout: int = 0,
         rc.mask, rc.lkout, rc.efdc_basetime, rc.max_samples = _ptr(m, _ip), lkout, efdc_basetime, max_samples
         wc = L.sw2dref_water_cells(R, Cc, _ptr(m, _ip))
     rc.nthreads = nthreads
-    outs = {k: np.zeros(N) for k in ("h", "um", "vn", "uu", "vv", "uua", "vva")}
+    rc.warm_iters = warm_iters
+    outs = {k: np.zeros(N) for k in (("h", "um", "vn", "uu", "vv", "uua", "vva") if want_fields else ("h",))}
     ro = RefOut()
     for k, a in outs.items():
         setattr(ro, k, _ptr(a, _dp))
@@ -341,6 +344,7 @@ def run_reference(case: Case, nthreads: int = 1, mask=None, lkout: int = 0,
     res = {k: v[: R * Cc].reshape(R, Cc) for k, v in outs.items()}
     res["iters"] = ro.iters
     res["time"] = ro.time
+    res["loop_seconds"] = ro.loop_seconds
     if mask is not None:
         res["water_cells"] = ro.water_cells
         res["nqs"] = ro.nqs

@@ -64,6 +64,7 @@ typedef struct sw2dref_case {
     double efdc_basetime;
     int max_samples;       /* rows of *_val the caller reserved */
     int nthreads;
+    int warm_iters;        /* iterations excluded from loop_seconds */
 } sw2dref_case;
 
 typedef struct sw2dref_out {
@@ -75,6 +76,7 @@ typedef struct sw2dref_out {
     int nsamples;            /* tq + 1 */
     int* bc;                 /* 4 sides (N,S,E,W) x water_cells x 3, or NULL */
     double* val;             /* 4 sides x max_samples x (water_cells+1), or NULL */
+    double loop_seconds;     /* wall time of the iterations after warm_iters */
 } sw2dref_out;
 
 int sw2dref_water_cells(int rows, int cols, const int* mask) {
@@ -156,7 +158,9 @@ int sw2dref_run(const sw2dref_case* c, sw2dref_out* o) {
     double time = c->time0;
     int mstep = 0, tq = -1, out0 = -1;
     long long iters = 0;
+    double wall0 = omp_get_wtime();
     while (time + dt <= c->timmax) {               /* SW2D-EFDC.cu:4798 */
+        if (iters == c->warm_iters) wall0 = omp_get_wtime();
         out0 = out0 + 1;
         REF_LAUNCH(flux, &th, gg, c->manning, inf.data(), h.data(), infx.data(), infy.data(),
                    baseo.data(), um.data(), hm.data(), uu1.data(), umo.data(), vv1.data(),
@@ -212,6 +216,7 @@ int sw2dref_run(const sw2dref_case* c, sw2dref_out* o) {
         }
     }
 
+    o->loop_seconds = omp_get_wtime() - wall0;
     double* outs[7] = {o->h, o->um, o->vn, o->uu, o->vv, o->uua, o->vva};
     const std::vector<double>* srcs[7] = {&h, &um, &vn, &uu, &vv, &uua, &vva};
     for (int k = 0; k < 7; k++)

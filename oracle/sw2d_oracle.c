@@ -411,11 +411,16 @@ static void update_face_velocities(orc_state* s) {
     }
 }
 
-/* CFL speed sum max over wet cells of (|u|+c)/dx + (|v|+c)/dy, with the
- * reference's cell velocities (uu_vv :468-476) and c = sqrt(g h). */
+/* CFL speed of the state (h, qx, qy): the maximum over active cells with
+ * h >= th of
+ *     (|qxc| / dx + |qyc| / dy) / h + sqrt(g h) (1/dx + 1/dy),
+ * qxc, qyc the means of the cell's two x-face and two y-face discharges.
+ * The iteration length is then min(dt_max, cfl / max).  The reference has
+ * no CFL control (its dt is fixed, SW2D-EFDC.cu:3770-3771); this is the
+ * rule the GPU step evaluates too, with the same operations. */
 static double cfl_speed(const orc_state* s) {
     const double th = s->c.th, g = s->c.g;
-    const double rdx = 1.0 / s->c.dx, rdy = 1.0 / s->c.dy;
+    const double rdx = 1.0 / s->c.dx, rdy = 1.0 / s->c.dy, rsum = rdx + rdy;
     const int P = s->P;
     double m = 0.0;
     for (int r = 0; r < s->R; r++)
@@ -423,10 +428,9 @@ static double cfl_speed(const orc_state* s) {
             size_t i = IX(s, r, c);
             double hh = s->h[i];
             if (!(s->act[i] && hh >= th)) continue;
-            double u = (s->uu1[i + P] + s->uu1[i]) / 2.00;
-            double v = (s->vv1[i + 1] + s->vv1[i]) / 2.00;
-            double cw = sqrt(g * hh);
-            double sp = (fabs(u) + cw) * rdx + (fabs(v) + cw) * rdy;
+            double qxc = 0.5 * (s->qx[i] + s->qx[i + P]);
+            double qyc = 0.5 * (s->qy[i] + s->qy[i + 1]);
+            double sp = (fabs(qxc) * rdx + fabs(qyc) * rdy) / hh + sqrt(g * hh) * rsum;
             if (sp > m) m = sp;
         }
     return m;

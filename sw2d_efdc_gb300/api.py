@@ -1,0 +1,301 @@
+"""Python mirror of the C ABI in include/sw2d.h (ctypes over libsw2d.so).
+
+This is plumbing for tests, the benchmark and Python callers: every call goes
+straight to the CUDA library; there is no CPU implementation behind it.  If
+the library is missing or no sm_103 GPU is present, the calls raise.
+
+Fields are numpy arrays in the reference orientation (row 0 = first ESRI row,
+north), as SW2D-EFDC.cu reads dem.dat (SW2D-EFDC.cu:3983-4003).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libsw2d.so")
+
+FP64, FP32 = 0, 1
+DT_FIXED, DT_CFL = 0, 1
+SERIES_REFERENCE, SERIES_LINEAR, SERIES_STEP = 0, 1, 2
+OUTFLOW_NONE, OUTFLOW_SOUTH = 0, 1
+
+STATUS = {
+    0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "invalid state",
+    -5: "HBM budget exceeded", -6: "non-finite state", -7: "no sm_103 device", -8: "timeout",
+    -9: "not found",
+}
+
+
+class Sw2dError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str):
+        super().__init__("%s failed: %s (%d): %s" % (where, STATUS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("rows", C.c_int), ("cols", C.c_int), ("precision", C.c_int), ("dt_mode", C.c_int),
+        ("series_mode", C.c_int), ("outflow", C.c_int), ("device", C.c_int), ("reserved0", C.c_int),
+        ("dx", C.c_double), ("dy", C.c_double), ("nodata", C.c_double), ("th", C.c_double),
+        ("g", C.c_double), ("manning", C.c_double), ("dt", C.c_double), ("cfl", C.c_double),
+        ("dt_max", C.c_double), ("t0", C.c_double), ("frac_int", C.c_double),
+        ("frac_inf", C.c_double), ("frac_lwl", C.c_double), ("ev_wl_min", C.c_double),
+        ("hbm_budget_bytes", C.c_double),
+    ]
+
+
+class Ledger(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "time", "iterations", "volume", "volume0", "rain_in", "source_in", "evap_out", "outflow",
+        "clamp_gain", "q_out", "s_max", "dt_last", "balance_error")]
+
+
+_dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int)
+_u8p = C.POINTER(C.c_uint8)
+_i64p = C.POINTER(C.c_int64)
+
+# name -> (restype, argtypes); every symbol include/sw2d.h declares
+SIGNATURES = {
+    "sw2d_abi_version": (C.c_int, []),
+    "sw2d_last_error": (C.c_char_p, []),
+    "sw2d_status_string": (C.c_char_p, [C.c_int]),
+    "sw2d_config_default": (C.c_int, [C.POINTER(Config)]),
+    "sw2d_create": (C.c_int, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
+    "sw2d_destroy": (C.c_int, [C.c_void_p]),
+    "sw2d_set_dem": (C.c_int, [C.c_void_p, _dp]),
+    "sw2d_set_depth": (C.c_int, [C.c_void_p, _dp]),
+    "sw2d_set_manning_classes": (C.c_int, [C.c_void_p, _u8p, _dp, C.c_int]),
+    "sw2d_set_rain_series": (C.c_int, [C.c_void_p, _dp, C.c_int, C.c_double]),
+    "sw2d_set_rain_field": (C.c_int, [C.c_void_p, _fp]),
+    "sw2d_set_evaporation_series": (C.c_int, [C.c_void_p, _dp, C.c_int]),
+    "sw2d_set_point_sources": (C.c_int, [C.c_void_p, C.c_int, _ip, _dp, C.c_int, C.c_double]),
+    "sw2d_advance": (C.c_int, [C.c_void_p, C.c_double, _i64p]),
+    "sw2d_step": (C.c_int, [C.c_void_p, C.c_int, C.c_double]),
+    "sw2d_get_time": (C.c_int, [C.c_void_p, _dp, _i64p]),
+    "sw2d_get_state": (C.c_int, [C.c_void_p, _dp, _dp, _dp]),
+    "sw2d_get_velocity": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "sw2d_get_face_velocity": (C.c_int, [C.c_void_p, _dp, _dp]),
+    "sw2d_get_ledger": (C.c_int, [C.c_void_p, C.POINTER(Ledger)]),
+    "sw2d_set_outlet_record": (C.c_int, [C.c_void_p, C.c_int]),
+    "sw2d_get_outlet": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int, _ip]),
+    "sw2d_set_coupling_mask": (C.c_int, [C.c_void_p, _ip, C.c_int, _ip]),
+    "sw2d_get_coupling_faces": (C.c_int, [C.c_void_p, _ip, _ip, _ip, _ip, C.c_int]),
+    "sw2d_couple_sample": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_int]),
+    "sw2d_snapshot_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "sw2d_snapshot": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "sw2d_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "sw2d_get_timing": (C.c_int, [C.c_void_p, _dp, _dp, _ip]),
+    "sw2d_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libsw2d.so; raises if it is missing (no fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError("libsw2d.so not built: run sw2d_efdc_gb300/build.py (or __graft_entry__.build())")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def _check(code: int, where: str):
+    if code != 0:
+        raise Sw2dError(code, where, load().sw2d_last_error().decode(errors="replace"))
+
+
+def default_config(**kw) -> Config:
+    cfg = Config()
+    _check(load().sw2d_config_default(C.byref(cfg)), "sw2d_config_default")
+    for k, v in kw.items():
+        if not hasattr(cfg, k):
+            raise KeyError(k)
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Model:
+    """One SW2D raster on one GPU (an sw2d_handle)."""
+
+    def __init__(self, cfg: Config):
+        L = load()
+        h = C.c_void_p()
+        _check(L.sw2d_create(C.byref(cfg), C.byref(h)), "sw2d_create")
+        self._h = h
+        self.cfg = cfg
+        self.rows, self.cols = cfg.rows, cfg.cols
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().sw2d_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _grid(self, a, dtype):
+        a = np.ascontiguousarray(a, dtype=dtype)
+        if a.shape != (self.rows, self.cols):
+            raise ValueError("expected shape %s, got %s" % ((self.rows, self.cols), a.shape))
+        return a
+
+    def set_dem(self, z):
+        z = self._grid(z, np.float64)
+        _check(load().sw2d_set_dem(self._h, _ptr(z, _dp)), "sw2d_set_dem")
+
+    def set_depth(self, d):
+        d = self._grid(d, np.float64)
+        _check(load().sw2d_set_depth(self._h, _ptr(d, _dp)), "sw2d_set_depth")
+
+    def set_manning_classes(self, classes, table):
+        if classes is None:
+            _check(load().sw2d_set_manning_classes(self._h, None, None, 0), "sw2d_set_manning_classes")
+            return
+        cl = self._grid(classes, np.uint8)
+        tb = np.ascontiguousarray(table, np.float64)
+        _check(load().sw2d_set_manning_classes(self._h, _ptr(cl, _u8p), _ptr(tb, _dp), len(tb)),
+               "sw2d_set_manning_classes")
+
+    def set_rain_series(self, mm, dtrain):
+        mm = np.ascontiguousarray(mm, np.float64)
+        _check(load().sw2d_set_rain_series(self._h, _ptr(mm, _dp), len(mm), float(dtrain)),
+               "sw2d_set_rain_series")
+
+    def set_rain_field(self, w):
+        w = None if w is None else self._grid(w, np.float32)
+        _check(load().sw2d_set_rain_field(self._h, _ptr(w, _fp)), "sw2d_set_rain_field")
+
+    def set_evaporation_series(self, mm):
+        mm = np.ascontiguousarray(mm, np.float64)
+        _check(load().sw2d_set_evaporation_series(self._h, _ptr(mm, _dp), len(mm)),
+               "sw2d_set_evaporation_series")
+
+    def set_point_sources(self, cells, q, dtoq):
+        cells = np.ascontiguousarray(cells, np.int32)
+        q = np.ascontiguousarray(q, np.float64)
+        nq = q.shape[0] if len(cells) else 0
+        _check(load().sw2d_set_point_sources(self._h, len(cells), _ptr(cells, _ip), _ptr(q, _dp), nq,
+                                             float(dtoq)), "sw2d_set_point_sources")
+
+    def advance(self, t_end) -> int:
+        n = C.c_int64(0)
+        _check(load().sw2d_advance(self._h, float(t_end), C.byref(n)), "sw2d_advance")
+        return n.value
+
+    def step(self, n, t_end=1e300):
+        _check(load().sw2d_step(self._h, int(n), float(t_end)), "sw2d_step")
+
+    def time(self):
+        t = C.c_double()
+        n = C.c_int64()
+        _check(load().sw2d_get_time(self._h, C.byref(t), C.byref(n)), "sw2d_get_time")
+        return t.value, n.value
+
+    def state(self):
+        R, Cc = self.rows, self.cols
+        h = np.empty((R, Cc))
+        qx = np.empty((R + 1, Cc))
+        qy = np.empty((R, Cc + 1))
+        _check(load().sw2d_get_state(self._h, _ptr(h, _dp), _ptr(qx, _dp), _ptr(qy, _dp)), "sw2d_get_state")
+        return h, qx, qy
+
+    def depth(self):
+        h = np.empty((self.rows, self.cols))
+        _check(load().sw2d_get_state(self._h, _ptr(h, _dp), None, None), "sw2d_get_state")
+        return h
+
+    def velocity(self):
+        uu = np.empty((self.rows, self.cols))
+        vv = np.empty((self.rows, self.cols))
+        _check(load().sw2d_get_velocity(self._h, _ptr(uu, _dp), _ptr(vv, _dp)), "sw2d_get_velocity")
+        return uu, vv
+
+    def face_velocity(self):
+        a = np.empty((self.rows, self.cols))
+        b = np.empty((self.rows, self.cols))
+        _check(load().sw2d_get_face_velocity(self._h, _ptr(a, _dp), _ptr(b, _dp)), "sw2d_get_face_velocity")
+        return a, b
+
+    def ledger(self) -> dict:
+        L = Ledger()
+        _check(load().sw2d_get_ledger(self._h, C.byref(L)), "sw2d_get_ledger")
+        return {n: getattr(L, n) for n, _ in Ledger._fields_}
+
+    def set_outlet_record(self, capacity):
+        _check(load().sw2d_set_outlet_record(self._h, int(capacity)), "sw2d_set_outlet_record")
+
+    def outlet(self, capacity=1 << 20):
+        n = C.c_int(0)
+        _check(load().sw2d_get_outlet(self._h, None, None, 0, C.byref(n)), "sw2d_get_outlet")
+        m = min(n.value, capacity)
+        t = np.empty(m)
+        q = np.empty(m)
+        _check(load().sw2d_get_outlet(self._h, _ptr(t, _dp), _ptr(q, _dp), m, C.byref(n)), "sw2d_get_outlet")
+        return t, q
+
+    def set_coupling_mask(self, mask, lagged=True) -> int:
+        m = self._grid(mask, np.int32)
+        n = C.c_int(0)
+        _check(load().sw2d_set_coupling_mask(self._h, _ptr(m, _ip), int(bool(lagged)), C.byref(n)),
+               "sw2d_set_coupling_mask")
+        self._nfaces = n.value
+        return n.value
+
+    def coupling_faces(self):
+        n = self._nfaces
+        side, fi, fj, cell = (np.zeros(n, np.int32) for _ in range(4))
+        _check(load().sw2d_get_coupling_faces(self._h, _ptr(side, _ip), _ptr(fi, _ip), _ptr(fj, _ip),
+                                              _ptr(cell, _ip), n), "sw2d_get_coupling_faces")
+        return side, fi, fj, cell
+
+    def couple_sample(self, initial=False):
+        q = np.zeros(self._nfaces)
+        _check(load().sw2d_couple_sample(self._h, int(bool(initial)), _ptr(q, _dp), self._nfaces),
+               "sw2d_couple_sample")
+        return q
+
+    def snapshot(self) -> bytes:
+        n = C.c_size_t(0)
+        _check(load().sw2d_snapshot_size(self._h, C.byref(n)), "sw2d_snapshot_size")
+        buf = C.create_string_buffer(n.value)
+        _check(load().sw2d_snapshot(self._h, buf, n.value), "sw2d_snapshot")
+        return buf.raw
+
+    def restore(self, data: bytes):
+        buf = C.create_string_buffer(data, len(data))
+        _check(load().sw2d_restore(self._h, buf, len(data)), "sw2d_restore")
+
+    def set_profiling(self, on=True):
+        _check(load().sw2d_set_profiling(self._h, int(bool(on))), "sw2d_set_profiling")
+
+    def timing(self):
+        ms = C.c_double()
+        per = np.zeros(8)
+        nk = C.c_int()
+        _check(load().sw2d_get_timing(self._h, C.byref(ms), _ptr(per, _dp), C.byref(nk)), "sw2d_get_timing")
+        return ms.value, per[: nk.value]

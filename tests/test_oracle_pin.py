@@ -1,0 +1,121 @@
+"""The oracle's reference flavour against the reference's own kernels built
+for the CPU (oracle/_ref): bit-identical depths, discharges and velocities."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import bumpy_case
+
+ref_missing = O.ref_lib() is None
+pytestmark = pytest.mark.skipif(ref_missing, reason="reference CPU build unavailable")
+
+
+def _pin(case, **kw):
+    ref = O.run_reference(case, nthreads=4, **kw)
+    o = O.Oracle(case, math=O.MATH_LIBM)
+    n = o.run()
+    f = o.fields()
+    R = case.rows
+    assert n == ref["iters"] and o.time == ref["time"]
+    pairs = {"h": (f["h"], ref["h"]), "um": (f["qx"][:R], ref["um"]), "vn": (f["qy"][:, :case.cols], ref["vn"]),
+             "uu": (f["uu"], ref["uu"]), "vv": (f["vv"], ref["vv"]), "uua": (f["uua"], ref["uua"]),
+             "vva": (f["vva"], ref["vva"])}
+    for k, (a, b) in pairs.items():
+        assert np.array_equal(a, b), "%s: max diff %.3e" % (k, np.abs(a - b).max())
+    return o, ref
+
+
+def test_pin_basic_nodata_ponds_rain():
+    o, ref = _pin(bumpy_case())
+    assert ref["h"].max() > 0.1
+
+
+def test_pin_nonzero_initial_depth_on_nodata_cells():
+    case = bumpy_case(seed=8)
+    case.h0[case.dem == -9999.0] = 0.7  # the reference keeps them, the restatement zeroes them
+    _pin(case)
+
+
+def test_pin_runoff_fractions_and_ramp():
+    case = bumpy_case(R=30, C=26, seed=12, frac_int=0.2, frac_inf=0.15, frac_lwl=0.4, ev_wl_min=0.02,
+                      rain=np.array([6.0, 6.0, 6.0, 6.0]), dtrain=7.3, t_end=20.0, dt=0.05)
+    _pin(case)
+
+
+def test_pin_evaporation_series():
+    T = np.array([20.0, 24.0, 27.0, 22.0, 18.0, 21.0])
+    Rg = np.array([300.0, 600.0, 800.0, 500.0, 100.0, 0.0])
+    albedo = 0.08
+    case = bumpy_case(R=28, C=24, seed=13, ev_wl_min=0.01, rain=np.array([4.0] * 6), dtrain=3.7,
+                      t_end=12.0, dt=0.05)
+    # the oracle takes the evaporation series the reference's gpu_evaporation_calc produces
+    Rs = (1 - albedo) * Rg
+    pw = (999.85308 + 6.32693 * (0.01) * T - 8.523829 * (0.001) * T * T + 6.943248 * (0.00001) * T * T * T
+          - 3.821216 * (0.0000001) * T * T * T * T)
+    lv = (((T + 273.15) / ((T + 273.15) - 33.91)) * ((T + 273.15) / ((T + 273.15) - 33.91))) * 1.91846 * 1000000
+    ev = (Rs / (lv * pw)) * case.dtrain * 1000.0
+    case.evap = np.maximum(ev, 0)
+    _pin(case, evap_inputs=(T, Rg, albedo))
+
+
+def test_pin_point_sources():
+    case = bumpy_case(R=30, C=28, seed=14, rain=np.array([2.0] * 4), dtrain=3600.0, t_end=30.0, dt=0.05)
+    # reference coordinates: cell id = qiny*cols + qinx + 1 with qinx = round(|x0 - brx|),
+    # qiny = rows - round(|y0 - bry|) (SW2D-EFDC.cu:540-544)
+    brx = np.array([6.0, 15.0])
+    bry = np.array([20.0, 7.0])
+    qq = np.array([[0.6, -0.05], [0.9, -0.1], [0.3, 0.0], [0.0, 0.0]])
+    dtoq = 9.1
+    R, Cc = case.rows, case.cols
+    cells = []
+    for x, y in zip(brx, bry):
+        qinx = round(abs(0.0 - x))
+        qiny = R - round(abs(0.0 - y))
+        cells.append(qiny * Cc + qinx + 1)
+    case.src_cell = np.array(cells, np.int32)
+    case.src_q = qq
+    case.dtoq = dtoq
+    _pin(case, sources=(brx, bry, qq, dtoq, 0.0, 0.0))
+
+
+def test_pin_coupling_samples():
+    case = bumpy_case(R=34, C=30, seed=15, holes=False, t_end=9.0, dt=0.05)
+    mask = np.zeros(case.dem.shape, np.int32)
+    mask[10:20, 8:22] = 1
+    mask[0:2, 12:16] = 1
+    lkout = 20
+    max_samples = 16
+    ref = O.run_reference(case, nthreads=2, mask=mask, lkout=lkout, efdc_basetime=3600.0,
+                          max_samples=max_samples)
+    side, ci, cj, cell = O.couple_faces(mask)
+    # per-side lists in the reference's arrays
+    for s in range(4):
+        sel = side == s
+        nb = sel.sum()
+        got = np.stack([ci[sel], cj[sel], np.arange(1, nb + 1)], axis=1)
+        assert np.array_equal(ref["bc"][s][:nb], got)
+        assert not ref["bc"][s][nb:].any()
+    # replay the samples with the oracle and the reference's lag
+    o = O.Oracle(case, math=O.MATH_LIBM)
+    prev = None
+    t = 0
+    mstep = 0
+    tq = -1
+    first = True
+    while o.step():
+        mstep += 2
+        if mstep % lkout == 0 or first:
+            tq += 1
+            f = o.fields()
+            if first:
+                q = np.zeros(len(side))
+            else:
+                q = O.couple_values(*case.dem.shape, case.cellsize, case.cellsize, side, cell, f["h"],
+                                    prev["uua"], prev["vva"])
+            for s in range(4):
+                sel = side == s
+                nb = sel.sum()
+                assert np.array_equal(ref["val"][s][tq][1:nb + 1], q[sel]), (tq, s)
+            prev = f
+            first = False
+    assert tq + 1 == ref["nsamples"] > 3
