@@ -70,6 +70,8 @@ struct sw2d_handle {
     double* scratch = nullptr; /* 4 * rows * cols doubles, lazily */
     /* host mirrors */
     std::vector<uint8_t> host_flags;
+    std::vector<float> host_rainw;
+    double active_weight = 0.0; /* sum over active cells of the rain weight */
     bool have_dem = false, have_depth = false;
     int nrain = 0, nevap = 0, nsrc = 0, nq = 0, outlet_cap = 0;
     double dtrain = 3600.0, dtoq = 3600.0;
@@ -104,13 +106,15 @@ struct sw2d_handle {
         p.nq = nq;
         p.nblocks_cells = ((C + SW2D_BX - 1) / SW2D_BX) * ((R + SW2D_BY - 1) / SW2D_BY);
         p.outlet_cap = outlet_cap;
+        p.pct_lake = 1.00 - cfg.frac_lwl;                  /* SW2D-EFDC.cu:627 */
+        p.pct_land = 1.00 - (cfg.frac_int + cfg.frac_inf); /* SW2D-EFDC.cu:631 */
+        p.ledger_cells = (p.pct_lake != p.pct_land) || (nevap > 0);
+        p.rain_static = active_weight * p.pct_land;
         p.dx = cfg.dx;
         p.dy = cfg.dy;
         p.th = cfg.th;
         p.g = cfg.g;
         p.manning = cfg.manning;
-        p.pct_lake = 1.00 - cfg.frac_lwl;                  /* SW2D-EFDC.cu:627 */
-        p.pct_land = 1.00 - (cfg.frac_int + cfg.frac_inf); /* SW2D-EFDC.cu:631 */
         p.ev_wl_min = cfg.ev_wl_min;
         p.dtrain = dtrain;
         p.dtoq = dtoq;
@@ -145,6 +149,15 @@ struct sw2d_handle {
     }
 
     size_t pad_index(int r, int c) const { return (size_t)(r + SW2D_HALO) * P + (c + SW2D_HALO); }
+
+    void update_active_weight() {
+        double s = 0.0;
+        for (int r = 0; r < R; r++)
+            for (int c = 0; c < C; c++)
+                if (host_flags[pad_index(r, c)] & SW2D_F_ACTIVE)
+                    s += host_rainw.empty() ? 1.0 : (double)host_rainw[(size_t)r * C + c];
+        active_weight = s;
+    }
 };
 
 namespace {
@@ -510,6 +523,7 @@ int sw2d_set_dem(sw2d_handle* h, const double* zin) {
         /* source flags are re-applied by set_point_sources */
     }
     if ((rc = put(h, h->flags, h->host_flags.data(), h->ncell))) return rc;
+    h->update_active_weight();
     h->have_dem = true;
     h->graph_dirty = true;
     return SW2D_OK;
@@ -584,10 +598,13 @@ int sw2d_set_rain_field(sw2d_handle* h, const float* w) {
     if (rc) return rc;
     if (!w) {
         dfree(h->rainw);
+        h->host_rainw.clear();
     } else {
         if (!h->rainw && (rc = dalloc(&h->rainw, h->ncell))) return rc;
         if ((rc = upload_interior(h, h->rainw, w, h->R, h->C))) return rc;
+        h->host_rainw.assign(w, w + (size_t)h->R * h->C);
     }
+    h->update_active_weight();
     h->graph_dirty = true;
     return SW2D_OK;
 }
@@ -702,6 +719,7 @@ int sw2d_get_ledger(sw2d_handle* h, sw2d_ledger* out) {
     if (!h || !out) return fail(SW2D_ERR_INVALID, "null argument");
     int rc = set_device(h);
     if (rc) return rc;
+    if (h->have_depth && (rc = prime(h, 1))) return rc; /* volume of the current state */
     DevClock c;
     if ((rc = read_clock(h, &c))) return rc;
     out->time = c.t;

@@ -325,49 +325,105 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_hstar(StepParams p, int
 }
 
 /* ------------------------------------------------------------------------ */
-/* deterministic block reductions                                            */
+/* block reductions (fixed order: deterministic for a given grid)            */
 
-template <int NV>
-__device__ __forceinline__ void block_reduce(double (&v)[NV], int nmax_last) {
-    /* sums for v[0..NV-2] ... the last nmax_last entries are maxima */
-    __shared__ double sm[NV][SW2D_BX * SW2D_BY / 32];
-    const int lane = (threadIdx.y * SW2D_BX + threadIdx.x) & 31;
-    const int warp = (threadIdx.y * SW2D_BX + threadIdx.x) >> 5;
+#define NWARP (SW2D_BX * SW2D_BY / 32)
+
+__device__ __forceinline__ int tid_linear() { return threadIdx.y * SW2D_BX + threadIdx.x; }
+
+__device__ __forceinline__ double block_sum(double v, double* sm) {
+    const int lane = tid_linear() & 31, warp = tid_linear() >> 5;
 #pragma unroll
-    for (int k = 0; k < NV; k++) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            double t = __shfl_down_sync(0xffffffffu, v[k], o);
-            v[k] = (k >= NV - nmax_last) ? fmax(v[k], t) : v[k] + t;
-        }
-    }
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < NV; k++) sm[k][warp] = v[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     __syncthreads();
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    double t = 0.0;
     if (warp == 0) {
-        const int nw = SW2D_BX * SW2D_BY / 32;
+        t = lane < NWARP ? sm[lane] : 0.0;
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-            double t = lane < nw ? sm[k][lane] : 0.0;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                double u = __shfl_down_sync(0xffffffffu, t, o);
-                t = (k >= NV - nmax_last) ? fmax(t, u) : t + u;
-            }
-            v[k] = t;
-        }
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
     }
+    return t; /* valid in thread 0 */
 }
 
-#define NRED 7 /* vol, rain, clamp, evap, qout, (spare), smax */
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* sm) {
+    const int lane = tid_linear() & 31, warp = tid_linear() >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long u = __shfl_down_sync(0xffffffffu, v, o);
+        v = u > v ? u : v;
+    }
+    __syncthreads();
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    unsigned long long t = 0;
+    if (warp == 0) {
+        t = lane < NWARP ? sm[lane] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long u = __shfl_down_sync(0xffffffffu, t, o);
+            t = u > t ? u : t;
+        }
+    }
+    return t; /* valid in thread 0 */
+}
+
+__device__ __forceinline__ float block_max_f32_all(float v, float* sm) {
+    const int lane = tid_linear() & 31, warp = tid_linear() >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    float t = sm[0];
+#pragma unroll
+    for (int k = 1; k < NWARP; k++) t = fmaxf(t, sm[k]);
+    return t; /* valid in every thread */
+}
+
+/* CFL speed of a wet cell (the oracle's cfl_speed, same operations) */
+__device__ __forceinline__ double cell_speed(const StepParams& p, double fN, double fS, double fW, double fE,
+                                             double hh) {
+    const double qxc = 0.5 * (fN + fS);
+    const double qyc = 0.5 * (fW + fE);
+    return (fabs(qxc) * p.rdx + fabs(qyc) * p.rdy) / hh + sqrt(p.g * hh) * p.rsum;
+}
+
+/* binary32 estimate of cell_speed (relative error < 1e-6), used to select
+ * the few cells per block whose exact speed can be the block maximum */
+__device__ __forceinline__ float cell_speed_f32(const StepParams& p, double fN, double fS, double fW, double fE,
+                                                double hh) {
+    const float h = (float)hh;
+    const float qxc = 0.5f * ((float)fN + (float)fS);
+    const float qyc = 0.5f * ((float)fW + (float)fE);
+    return (fabsf(qxc) * (float)p.rdx + fabsf(qyc) * (float)p.rdy) / h + sqrtf((float)p.g * h) * (float)p.rsum;
+}
+
+/* Exact block maximum of the speed: binary32 prefilter, binary64 for the
+ * candidates within 1e-5 of the block's binary32 maximum, maximum over the
+ * IEEE bit patterns (the speeds are non-negative). */
+__device__ __forceinline__ unsigned long long block_speed_max(const StepParams& p, bool wet, double fN, double fS,
+                                                              double fW, double fE, double hh) {
+    __shared__ float smf[NWARP];
+    __shared__ unsigned long long smu[NWARP];
+    const float s32 = wet ? cell_speed_f32(p, fN, fS, fW, fE, hh) : 0.0f;
+    const float m32 = block_max_f32_all(s32, smf);
+    unsigned long long bits = 0ull;
+    if (wet && s32 >= m32 * 0.99999f) bits = (unsigned long long)__double_as_longlong(cell_speed(p, fN, fS, fW, fE, hh));
+    return block_max_u64(bits, smu);
+}
+
+#define NPART 4 /* rain, evap, qout, s_max bits */
 
 /* Final reduction over the per-block partials by the last block to finish,
  * then the iteration's ledger update and the next slot. */
 __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
     __shared__ bool last;
+    __shared__ double smd[NWARP];
+    __shared__ unsigned long long smu[NWARP];
     __threadfence();
-    const int tid = threadIdx.y * SW2D_BX + threadIdx.x;
+    const int tid = tid_linear();
     if (tid == 0) {
         unsigned int ticket = atomicAdd(&p.clk->counter, 1u);
         last = (ticket == (unsigned)nblocks - 1);
@@ -375,34 +431,41 @@ __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
     __syncthreads();
     if (!last) return;
     __threadfence();
-    double v[NRED];
-#pragma unroll
-    for (int k = 0; k < NRED; k++) v[k] = 0.0;
+    double vr = 0.0, ve = 0.0, vq = 0.0;
+    unsigned long long vs = 0ull;
     for (int b = tid; b < nblocks; b += SW2D_BX * SW2D_BY) {
-        const volatile double* pb = p.partials + (size_t)b * 8;
-#pragma unroll
-        for (int k = 0; k < NRED; k++) v[k] = (k == NRED - 1) ? fmax(v[k], pb[k]) : v[k] + pb[k];
+        const volatile double* pb = p.partials + (size_t)b * NPART;
+        vr += pb[0];
+        ve += pb[1];
+        vq += pb[2];
+        unsigned long long u = (unsigned long long)__double_as_longlong(pb[3]);
+        vs = u > vs ? u : vs;
     }
-    block_reduce<NRED>(v, 1);
+    if (p.ledger_cells) {
+        vr = block_sum(vr, smd);
+        ve = block_sum(ve, smd);
+    }
+    if (p.outflow_south) vq = block_sum(vq, smd);
+    vs = block_max_u64(vs, smu);
     if (tid == 0) {
         DevClock* clk = p.clk;
         const Slot& s = clk->slot[cur];
         if (s.active) {
             const double dt2 = s.dt2;
+            const double smax = __longlong_as_double((long long)vs);
             double src = 0.0;
             for (int k = 0; k < p.nsrc; k++) src += s.ql2[k];
-            clk->led[LED_VOLUME] = v[0] * p.area;
-            clk->led[LED_RAIN] += dt2 * v[1] * p.area;
-            clk->led[LED_CLAMP] += v[2] * p.area;
-            clk->led[LED_EVAP] += dt2 * v[3] * p.area;
+            const double rain = p.ledger_cells ? vr : s.rr2 * p.rain_static;
+            clk->led[LED_RAIN] += dt2 * rain * p.area;
+            clk->led[LED_EVAP] += dt2 * ve * p.area;
             clk->led[LED_SOURCE] += dt2 * src * p.area;
-            clk->led[LED_QOUT] = v[4] * p.dy;
+            clk->led[LED_QOUT] = vq * p.dy;
             clk->led[LED_OUTFLOW] += dt2 * clk->led[LED_QOUT];
             clk->led[LED_DTLAST] = dt2;
-            clk->led[LED_SMAX] = v[6];
-            if (!isfinite(v[0])) clk->status |= 1;
+            clk->led[LED_SMAX] = smax;
+            if (!isfinite(smax) || !isfinite(vq)) clk->status |= 1;
             clk->t = s.t_next;
-            clk->s_max = v[6];
+            clk->s_max = smax;
             clk->iters += 1;
             if (p.outlet) {
                 long long k = clk->outlet_n % p.outlet_cap;
@@ -419,13 +482,14 @@ __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
 }
 
 __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_depth(StepParams p, int cur) {
+    __shared__ double smd[NWARP];
     const int c = blockIdx.x * SW2D_BX + threadIdx.x;
     const int r = blockIdx.y * SW2D_BY + threadIdx.y;
     const int nxt = cur ^ 1;
     const Slot& s = p.clk->slot[cur];
-    double v[NRED];
-#pragma unroll
-    for (int k = 0; k < NRED; k++) v[k] = 0.0;
+    double vr = 0.0, ve = 0.0, vq = 0.0;
+    bool wet = false;
+    double fN = 0, fS = 0, fW = 0, fE = 0, hn = 0;
     if (r < p.R && c < p.C) {
         const int P = p.P;
         const size_t i = (size_t)(r + H) * P + (c + H);
@@ -439,37 +503,106 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_depth(StepParams p, int
             const uint8_t dc = d[i];
             /* treat_error per face: a face carrying water out of a cell whose
              * provisional depth fell below th is closed (:704-719) */
-            double fN = fx[i], fS = fx[i + P], fW = fy[i], fE = fy[i + 1];
+            fN = fx[i];
+            fS = fx[i + P];
+            fW = fy[i];
+            fE = fy[i + 1];
             if ((fN > 0 && d[i - P]) || (fN < 0 && dc)) fN = 0;
             if ((fS > 0 && dc) || (fS < 0 && d[i + P])) fS = 0;
             if ((fW > 0 && d[i - 1]) || (fW < 0 && dc)) fW = 0;
             if ((fE > 0 && dc) || (fE < 0 && d[i + 1])) fE = 0;
             const double ho = p.h[cur][i];
             double raw, rt;
-            const double hn = continuity(p, i, f, ho, fS - fN, fE - fW, s.dt2, s.rr2, s.ev2, s.ql2, &raw, &rt);
+            hn = continuity(p, i, f, ho, fS - fN, fE - fW, s.dt2, s.rr2, s.ev2, s.ql2, &raw, &rt);
             p.h[nxt][i] = hn;
             if (f & SW2D_F_ACTIVE) {
-                v[0] = hn;
-                v[1] = rt;
-                v[2] = hn - raw;
-                v[3] = (ho > p.ev_wl_min) ? s.ev2 : 0.0;
-                if (r == p.R - 1 && p.outflow_south) v[4] = fS;
-                if (hn >= p.th) {
-                    const double qxc = 0.5 * (fN + fS);
-                    const double qyc = 0.5 * (fW + fE);
-                    v[6] = (fabs(qxc) * p.rdx + fabs(qyc) * p.rdy) / hn + sqrt(p.g * hn) * p.rsum;
+                if (raw < 0) atomicAdd(&p.clk->led[LED_CLAMP], -raw * p.area); /* max(h, 0) gain */
+                if (p.ledger_cells) {
+                    vr = rt;
+                    ve = (ho > p.ev_wl_min) ? s.ev2 : 0.0;
                 }
+                if (r == p.R - 1) vq = fS;
+                wet = hn >= p.th;
             }
         }
     }
-    block_reduce<NRED>(v, 1);
-    const int tid = threadIdx.y * SW2D_BX + threadIdx.x;
+    double pr = 0.0, pe = 0.0, pq = 0.0;
+    if (p.ledger_cells) {
+        pr = block_sum(vr, smd);
+        pe = block_sum(ve, smd);
+    }
+    if (p.outflow_south && (blockIdx.y + 1) * SW2D_BY >= p.R) pq = block_sum(vq, smd);
+    const unsigned long long sb = (p.dt_mode == 1) ? block_speed_max(p, wet, fN, fS, fW, fE, hn) : 0ull;
+    const int tid = tid_linear();
     const int b = blockIdx.y * gridDim.x + blockIdx.x;
     if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < NRED; k++) p.partials[(size_t)b * 8 + k] = v[k];
+        double* pb = p.partials + (size_t)b * NPART;
+        pb[0] = pr;
+        pb[1] = pe;
+        pb[2] = pq;
+        pb[3] = __longlong_as_double((long long)sb);
     }
     finish_iteration(p, cur, gridDim.x * gridDim.y);
+}
+
+/* Volume (sum of h over active cells) and, with full, the CFL speed of the
+ * current state; the last block stores them and prepares the next slot. */
+__global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int cur, int full) {
+    __shared__ double smd[NWARP];
+    __shared__ unsigned long long smu[NWARP];
+    __shared__ bool last;
+    const int c = blockIdx.x * SW2D_BX + threadIdx.x;
+    const int r = blockIdx.y * SW2D_BY + threadIdx.y;
+    double vol = 0.0;
+    unsigned long long sb = 0ull;
+    if (full && r < p.R && c < p.C) {
+        const int P = p.P;
+        const size_t i = (size_t)(r + H) * P + (c + H);
+        const double hh = p.h[cur][i];
+        if ((p.flags[i] & SW2D_F_ACTIVE)) {
+            vol = hh;
+            if (hh >= p.th) {
+                const double* fx = p.qx[cur];
+                const double* fy = p.qy[cur];
+                sb = (unsigned long long)__double_as_longlong(cell_speed(p, fx[i], fx[i + P], fy[i], fy[i + 1], hh));
+            }
+        }
+    }
+    vol = block_sum(vol, smd);
+    sb = block_max_u64(sb, smu);
+    const int tid = tid_linear();
+    const int b = blockIdx.y * gridDim.x + blockIdx.x;
+    if (tid == 0) {
+        p.partials[(size_t)b * NPART + 0] = vol;
+        p.partials[(size_t)b * NPART + 3] = __longlong_as_double((long long)sb);
+    }
+    __threadfence();
+    if (tid == 0) last = (atomicAdd(&p.clk->counter, 1u) == gridDim.x * gridDim.y - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int nb = gridDim.x * gridDim.y;
+    double v = 0.0;
+    unsigned long long u = 0ull;
+    for (int bb = tid; bb < nb; bb += SW2D_BX * SW2D_BY) {
+        const volatile double* pb = p.partials + (size_t)bb * NPART;
+        v += pb[0];
+        unsigned long long w = (unsigned long long)__double_as_longlong(pb[3]);
+        u = w > u ? w : u;
+    }
+    v = block_sum(v, smd);
+    u = block_max_u64(u, smu);
+    if (tid == 0) {
+        DevClock* clk = p.clk;
+        if (full) {
+            clk->s_max = __longlong_as_double((long long)u);
+            clk->led[LED_SMAX] = clk->s_max;
+            clk->led[LED_VOLUME] = v * p.area;
+            if (full == 2) clk->led[LED_VOLUME0] = clk->led[LED_VOLUME];
+        }
+        prepare_slot(p, &clk->slot[cur], clk->t, clk->s_max, clk->t_end);
+        clk->counter = 0;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -497,7 +630,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, i
         if (r == 0) hm = h[i];
         else if (r == p.R) hm = h[i - P];
         else hm = 0.50 * (h[i] + h[i - P]);
-        p.uu1[i] = (hm >= th) ? F / hm : 0.00;
+        p.uu1[i] = (hm >= th) ? (F == 0 ? F : F / hm) : 0.00; /* 0/hm is 0 of F's sign */
     }
     if (r < p.R) {
         double F = p.qy[nxt][i];
@@ -510,63 +643,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, i
         if (c == 0) hn = h[i];
         else if (c == p.C) hn = h[i - 1];
         else hn = 0.50 * (h[i] + h[i - 1]);
-        p.vv1[i] = (hn >= th) ? F / hn : 0.0;
-    }
-}
-
-/* ------------------------------------------------------------------------ */
-/* CFL speed of a given state + first slot                                    */
-
-__global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int cur, int full) {
-    double v[NRED];
-#pragma unroll
-    for (int k = 0; k < NRED; k++) v[k] = 0.0;
-    const int c = blockIdx.x * SW2D_BX + threadIdx.x;
-    const int r = blockIdx.y * SW2D_BY + threadIdx.y;
-    if (full && r < p.R && c < p.C) {
-        const int P = p.P;
-        const size_t i = (size_t)(r + H) * P + (c + H);
-        const double hh = p.h[cur][i];
-        if ((p.flags[i] & SW2D_F_ACTIVE)) {
-            v[0] = hh;
-            if (hh >= p.th) {
-                const double* fx = p.qx[cur];
-                const double* fy = p.qy[cur];
-                const double qxc = 0.5 * (fx[i] + fx[i + P]);
-                const double qyc = 0.5 * (fy[i] + fy[i + 1]);
-                v[6] = (fabs(qxc) * p.rdx + fabs(qyc) * p.rdy) / hh + sqrt(p.g * hh) * p.rsum;
-            }
-        }
-    }
-    block_reduce<NRED>(v, 1);
-    const int tid = threadIdx.y * SW2D_BX + threadIdx.x;
-    const int b = blockIdx.y * gridDim.x + blockIdx.x;
-    if (tid == 0) {
-#pragma unroll
-        for (int k = 0; k < NRED; k++) p.partials[(size_t)b * 8 + k] = v[k];
-    }
-    __shared__ bool last;
-    __threadfence();
-    if (tid == 0) last = (atomicAdd(&p.clk->counter, 1u) == gridDim.x * gridDim.y - 1);
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    for (int k = 0; k < NRED; k++) v[k] = 0.0;
-    const int nb = gridDim.x * gridDim.y;
-    for (int bb = tid; bb < nb; bb += SW2D_BX * SW2D_BY) {
-        const volatile double* pb = p.partials + (size_t)bb * 8;
-        for (int k = 0; k < NRED; k++) v[k] = (k == NRED - 1) ? fmax(v[k], pb[k]) : v[k] + pb[k];
-    }
-    block_reduce<NRED>(v, 1);
-    if (tid == 0) {
-        DevClock* clk = p.clk;
-        if (full) {
-            clk->s_max = v[6];
-            clk->led[LED_SMAX] = v[6];
-            clk->led[LED_VOLUME] = v[0] * p.area;
-        }
-        prepare_slot(p, &clk->slot[cur], clk->t, clk->s_max, clk->t_end);
-        clk->counter = 0;
+        p.vv1[i] = (hn >= th) ? (F == 0 ? F : F / hn) : 0.0;
     }
 }
 

@@ -72,6 +72,8 @@ struct StepParams {
     int nsrc, nrain, nevap, nq;
     int nblocks_cells;     /* blocks of the cell-grid reduction kernels */
     int outlet_cap;
+    int ledger_cells;      /* 1: rain/evaporation volumes need a per-cell sum */
+    double rain_static;    /* else: sum over active cells of weight * runoff fraction */
     double dx, dy, th, g, manning;
     double pct_lake, pct_land, ev_wl_min;
     double dtrain, dtoq, dt_fixed, cfl, dt_max, rdx, rdy, rsum, area;

@@ -87,6 +87,7 @@ SW2D_HD float sw2d_fmaf(float a, float b, float c) { return fmaf(a, b, c); }
  * fma-based residual correction (Markstein's theorem: with rd = RN(1/d) the
  * corrected quotient is the correctly rounded a/d). */
 SW2D_HD double sw2d_div_const(double a, double d, double rd) {
+    if (a == 0.0) return 0.0; /* what the sequence below yields for +0 and -0 */
     double q = a * rd;
     double e = sw2d_fma(-q, d, a);
     return sw2d_fma(e, rd, q);
