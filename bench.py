@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Gcell-updates/s plain vs batched-FP32 on 1 GB300 at stated error; p50/p99 latency"
 UNIT = "Gcell-updates/s"
 BYTES_PER_CELL_FP64_CFG2 = 62  # h,qx,qy r+w 48 + z 8 + flag 1 + Manning class 1 + rain weight (fp32) 4
+BYTES_PER_CELL_FP32_CFG3 = 37  # h,qx,qy r+w 24 + z offset 4 + info byte 1 + Kahan compensation r+w 8
 
 
 def dist_env():
@@ -153,6 +154,44 @@ def cpu_reference_sample(sc, iters: int, warm: int, threads: int, h0=None):
     return sc.rows * sc.cols * n / secs / 1e9, secs, n
 
 
+def run_fp32_leg(args, peak):
+    """FP32 precision form on the 8192 x 8192 dx = 1 m tilted-plane raster with a
+    gamma hyetograph (the fused TMA tile kernel), spun up, then K iterations."""
+    from sw2d_efdc_gb300 import api, synth
+    size = args.fp32_size
+    sc = synth.config3(rows=size, cols=size)
+    cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=api.FP32, dt_mode=sc.dt_mode,
+                             series_mode=sc.series_mode, dx=sc.dx, dy=sc.dx, manning=sc.manning, cfl=sc.cfl,
+                             dt_max=sc.dt_max, outflow=api.OUTFLOW_SOUTH)
+    m = api.Model(cfg)
+    m.set_dem(sc.dem)
+    m.set_rain_series(sc.rain_mm, sc.dtrain)
+    m.set_depth(sc.h0)
+    m.advance(args.fp32_spinup_s)
+    t_spun = m.time()[0]
+    K = args.steps + (args.steps & 1)
+    m.step(max(args.warmup, 3))
+    m.step(K)
+    ms_iter, _ = m.timing()
+    cells = sc.rows * sc.cols
+    led = m.ledger()
+    m.close()
+    achieved = BYTES_PER_CELL_FP32_CFG3 * cells / (ms_iter * 1e-3) / 1e9
+    return {
+        "value": round(cells / (ms_iter * 1e-3) / 1e9, 4), "unit": UNIT, "ms_per_step": round(ms_iter, 4),
+        "steps": K, "dtype": "f32 (f64 clock, ledger, CFL length)",
+        "workload": "FP32 precision form %dx%d dx=1m tilted plane + bumps, gamma 5-min hyetograph "
+                    "(shape 0.8, mean 20 mm/h), CFL 0.7, free south outlet, timed from t=%.0f s"
+                    % (sc.rows, sc.cols, t_spun),
+        "roofline": {"bound": "hbm", "kernel": "k32_step (fused TMA tile) + k32_finalize",
+                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3,
+                     "traffic": None},
+        "balance_error": led["balance_error"],
+        "vs_fp64_plain": None,
+    }
+
+
 def run_ours(args):
     rank, local, world = dist_env()
     from sw2d_efdc_gb300 import api
@@ -250,6 +289,9 @@ def run_ours(args):
         "e2e": e2e,
         "ledger": {"time_s": led["time"], "iterations": led["iterations"], "dt_last": led["dt_last"]},
     }
+    if not args.no_fp32:
+        out["fp32_precision_form"] = run_fp32_leg(args, peak)
+        out["fp32_precision_form"]["vs_fp64_plain"] = round(out["fp32_precision_form"]["value"] / value, 3)
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, secs, n = cpu_reference_sample(sc, args.cpu_iters, 1, threads, h0=h_spun)
@@ -295,6 +337,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-kernel-split", action="store_true")
     ap.add_argument("--size", type=int, default=4096, help="raster side of the pond-break workload")
+    ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--fp32-size", type=int, default=8192)
+    ap.add_argument("--fp32-spinup-s", type=float, default=300.0)
+    ap.add_argument("--fp64-only", action="store_true")
     ap.add_argument("--spinup-s", type=float, default=60.0, help="simulated seconds before timing")
     ap.add_argument("--spinup-iters", type=int, default=0, help="iterations before timing (overrides --spinup-s)")
     args = ap.parse_args()

@@ -411,29 +411,39 @@ static void update_face_velocities(orc_state* s) {
     }
 }
 
-/* CFL speed of the state (h, qx, qy): the maximum over active cells with
- * h >= th of
- *     (|qxc| / dx + |qyc| / dy) / h + sqrt(g h) (1/dx + 1/dy),
- * qxc, qyc the means of the cell's two x-face and two y-face discharges.
- * The iteration length is then min(dt_max, cfl / max).  The reference has
- * no CFL control (its dt is fixed, SW2D-EFDC.cu:3770-3771); this is the
- * rule the GPU step evaluates too, with the same operations. */
+/* CFL speed of the state (h, qx, qy) with its face velocities uu1, vv1:
+ *     S = max over x faces of (|uu1| + sqrt(g hm)) / dx
+ *       + max over y faces of (|vv1| + sqrt(g hn)) / dy,
+ * over faces whose two cells are active and whose mean depth is >= th.
+ * An iteration's length is min(dt_max, cfl / S) with S of the state the
+ * PREVIOUS iteration started from (the first two iterations use the initial
+ * state), so the GPU can reduce S while it computes that iteration.  The
+ * reference has no CFL control (its dt is fixed, SW2D-EFDC.cu:3770-3771). */
 static double cfl_speed(const orc_state* s) {
     const double th = s->c.th, g = s->c.g;
-    const double rdx = 1.0 / s->c.dx, rdy = 1.0 / s->c.dy, rsum = rdx + rdy;
+    const double rdx = 1.0 / s->c.dx, rdy = 1.0 / s->c.dy;
     const int P = s->P;
-    double m = 0.0;
+    double mx = 0.0, my = 0.0;
     for (int r = 0; r < s->R; r++)
         for (int c = 0; c < s->C; c++) {
             size_t i = IX(s, r, c);
-            double hh = s->h[i];
-            if (!(s->act[i] && hh >= th)) continue;
-            double qxc = 0.5 * (s->qx[i] + s->qx[i + P]);
-            double qyc = 0.5 * (s->qy[i] + s->qy[i + 1]);
-            double sp = (fabs(qxc) * rdx + fabs(qyc) * rdy) / hh + sqrt(g * hh) * rsum;
-            if (sp > m) m = sp;
+            if (!s->act[i]) continue;
+            if (r > 0 && s->act[i - P]) {
+                double hm = 0.50 * (s->h[i] + s->h[i - P]);
+                if (hm >= th) {
+                    double sp = (fabs(s->uu1[i]) + sqrt(g * hm)) * rdx;
+                    if (sp > mx) mx = sp;
+                }
+            }
+            if (c > 0 && s->act[i - 1]) {
+                double hn = 0.50 * (s->h[i] + s->h[i - 1]);
+                if (hn >= th) {
+                    double sp = (fabs(s->vv1[i]) + sqrt(g * hn)) * rdy;
+                    if (sp > my) my = sp;
+                }
+            }
         }
-    return m;
+    return mx + my;
 }
 
 /* ---------------- one iteration: SW2D-EFDC.cu:4808-4877 ------------------ */
@@ -459,6 +469,7 @@ int orc_step(orc_state* s, double t_end) {
     }
     const double dt2dx = dt2 / s->c.dx, dt2dy = dt2 / s->c.dy;
     const int nt = s->c.nthreads > 0 ? s->c.nthreads : 1;
+    const double s_entering = (s->c.dt_mode == ORC_DT_CFL) ? cfl_speed(s) : 0.0;
 
     /* 1. flux (:4810) */
 #pragma omp parallel for num_threads(nt) schedule(static)
@@ -562,7 +573,7 @@ int orc_step(orc_state* s, double t_end) {
     s->t = t_next;
     s->iters++;
     if (s->c.dt_mode == ORC_DT_CFL) {
-        s->L.s_max = cfl_speed(s);
+        s->L.s_max = s_entering;
         s->dt2_next = s->L.s_max > 0 ? fmin(s->c.dt_max, s->c.cfl / s->L.s_max) : s->c.dt_max;
     }
     if (s->out_n == s->out_cap) {

@@ -27,9 +27,11 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path
 # translation unit -> extra flags
 UNITS = {
     "sw2d_fp64.cu": ["--fmad=false", "-Xptxas", "-v"],
+    "sw2d_fp32.cu": ["-Xptxas", "-v"],
+    "sw2d_engine.cu": [],
     "sw2d_api.cu": [],
 }
-HEADERS = ["sw2d_internal.h", "sw2d_math.h"]
+HEADERS = ["sw2d_internal.h", "sw2d_math.h", "sw2d_fp32.h", "sw2d_engine.h"]
 
 
 def nvcc() -> str:

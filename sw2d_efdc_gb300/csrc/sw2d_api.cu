@@ -8,12 +8,14 @@
  * until the loop condition is checked at the end of a chunk.
  */
 #include "sw2d.h"
+#include "sw2d_engine.h"
 #include "sw2d_internal.h"
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <memory>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -65,6 +67,7 @@ struct sw2d_handle {
     double* evap = nullptr;
     double* srcq = nullptr;
     double* partials = nullptr;
+    double* partials_f = nullptr;
     double* outlet = nullptr;
     DevClock* clk = nullptr;
     double* scratch = nullptr; /* 4 * rows * cols doubles, lazily */
@@ -91,6 +94,13 @@ struct sw2d_handle {
     double last_ms_per_iter = 0.0;
     std::vector<double> kernel_ms;
     long long prof_iters = 0;
+    /* FP32 precision form: a one-scenario engine built from host copies of the inputs */
+    std::unique_ptr<sw2d::Engine32> eng;
+    int eng_idx = -1;
+    std::vector<double> in_dem, in_depth, in_mtab, in_rain;
+    std::vector<uint8_t> in_mcls;
+    std::vector<float> in_rainw;
+    bool fp32() const { return cfg.precision == SW2D_FP32; }
 
     StepParams params() const {
         StepParams p{};
@@ -105,6 +115,7 @@ struct sw2d_handle {
         p.nevap = nevap;
         p.nq = nq;
         p.nblocks_cells = ((C + SW2D_BX - 1) / SW2D_BX) * ((R + SW2D_BY - 1) / SW2D_BY);
+        p.nblocks_faces = ((C + 1 + SW2D_BX - 1) / SW2D_BX) * ((R + 1 + SW2D_BY - 1) / SW2D_BY);
         p.outlet_cap = outlet_cap;
         p.pct_lake = 1.00 - cfg.frac_lwl;                  /* SW2D-EFDC.cu:627 */
         p.pct_land = 1.00 - (cfg.frac_int + cfg.frac_inf); /* SW2D-EFDC.cu:631 */
@@ -143,6 +154,7 @@ struct sw2d_handle {
         p.vv1 = vv1;
         p.drys = drys;
         p.partials = partials;
+        p.partials_f = partials_f;
         p.outlet = outlet;
         p.clk = clk;
         return p;
@@ -288,15 +300,89 @@ int launch_iterations(sw2d_handle* h, long long n) {
     return SW2D_OK;
 }
 
+int fp32_rebuild(sw2d_handle* h) {
+    if (h->eng_idx >= 0) {
+        h->eng->remove(h->eng_idx);
+        h->eng_idx = -1;
+    }
+    sw2d::ScenarioInput in;
+    const sw2d_config& c = h->cfg;
+    in.rows = c.rows;
+    in.cols = c.cols;
+    in.dx = c.dx;
+    in.dy = c.dy;
+    in.nodata = c.nodata;
+    in.th = c.th;
+    in.g = c.g;
+    in.manning = c.manning;
+    in.dt_mode = c.dt_mode;
+    in.series_mode = c.series_mode;
+    in.outflow_south = c.outflow == SW2D_OUTFLOW_SOUTH;
+    in.dt = c.dt;
+    in.cfl = c.cfl;
+    in.dt_max = c.dt_max;
+    in.t0 = c.t0;
+    in.t_end = c.t0;
+    in.frac_int = c.frac_int;
+    in.frac_inf = c.frac_inf;
+    in.frac_lwl = c.frac_lwl;
+    in.ev_wl_min = c.ev_wl_min;
+    in.dem = h->in_dem.data();
+    in.depth = h->in_depth.data();
+    if (!h->in_mcls.empty()) {
+        in.mclass = h->in_mcls.data();
+        in.mtable = h->in_mtab.data();
+        in.ntable = (int)h->in_mtab.size();
+    }
+    in.rain = h->in_rain.data();
+    in.nrain = (int)h->in_rain.size();
+    in.dtrain = h->dtrain;
+    if (!h->in_rainw.empty()) in.rain_weight = h->in_rainw.data();
+    in.outlet_cap = h->outlet_cap;
+    std::string err;
+    int rc = h->eng->add(in, 0, &err, &h->eng_idx);
+    if (rc) return fail(rc, err);
+    return SW2D_OK;
+}
+
 int check_ready(sw2d_handle* h) {
     if (!h) return fail(SW2D_ERR_INVALID, "null handle");
     if (!h->have_dem || !h->have_depth) return fail(SW2D_ERR_STATE, "set_dem and set_depth must be called first");
     return set_device(h);
 }
 
+int run_until_fp32(sw2d_handle* h, double t_end, long long max_iters, int64_t* done_out) {
+    std::string err;
+    int rc = h->eng->set_t_end(h->eng_idx, t_end, &err);
+    if (rc) return fail(rc, err);
+    sw2d::Clock32 c0, c;
+    if ((rc = h->eng->get_clock(h->eng_idx, &c0, &err))) return fail(rc, err);
+    double ms = 0;
+    if (max_iters >= 0) {
+        if ((rc = h->eng->run(max_iters, &err))) return fail(rc, err);
+        ms = h->eng->last_ms();
+    } else {
+        for (;;) {
+            if ((rc = h->eng->run(64, &err))) return fail(rc, err);
+            ms += h->eng->last_ms();
+            if ((rc = h->eng->get_clock(h->eng_idx, &c, &err))) return fail(rc, err);
+            if (c.done || !c.slot.active) break;
+            if (c.status & 3) break;
+        }
+    }
+    if ((rc = h->eng->get_clock(h->eng_idx, &c, &err))) return fail(rc, err);
+    const long long done = c.iters - c0.iters;
+    h->last_ms_per_iter = done > 0 ? ms / (double)done : 0.0;
+    if (done_out) *done_out = done;
+    if (c.status & 2) return fail(SW2D_ERR_TIMEOUT, "a tile's staged load did not arrive in time");
+    if (c.status & 1) return fail(SW2D_ERR_NUMERIC, "non-finite state");
+    return SW2D_OK;
+}
+
 int run_until(sw2d_handle* h, double t_end, long long max_iters, int64_t* done_out) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (h->fp32()) return run_until_fp32(h, t_end, max_iters, done_out);
     if ((rc = put(h, &h->clk->t_end, &t_end, sizeof(double)))) return rc;
     if ((rc = prime(h, 0))) return rc;
     DevClock c0;
@@ -400,7 +486,7 @@ int sw2d_create(const sw2d_config* cfg, sw2d_handle** out) {
     if ((long long)cfg->rows * cfg->cols > (1LL << 31) / 2) return fail(SW2D_ERR_INVALID, "raster too large");
     if (!(cfg->dx > 0) || !(cfg->dy > 0)) return fail(SW2D_ERR_INVALID, "dx, dy must be > 0");
     if (!(cfg->th > 0)) return fail(SW2D_ERR_INVALID, "th must be > 0");
-    if (cfg->precision != SW2D_FP64) return fail(SW2D_ERR_INVALID, "precision not available in this build");
+    if (cfg->precision != SW2D_FP64 && cfg->precision != SW2D_FP32) return fail(SW2D_ERR_INVALID, "precision");
     if (cfg->dt_mode == SW2D_DT_FIXED && !(cfg->dt > 0)) return fail(SW2D_ERR_INVALID, "dt must be > 0");
     if (cfg->dt_mode == SW2D_DT_CFL && (!(cfg->cfl > 0) || !(cfg->dt_max > 0)))
         return fail(SW2D_ERR_INVALID, "cfl and dt_max must be > 0");
@@ -415,6 +501,25 @@ int sw2d_create(const sw2d_config* cfg, sw2d_handle** out) {
         return fail(SW2D_ERR_NODEVICE, "this library is built for sm_103a (GB300) only");
     sw2d_handle* h = new sw2d_handle();
     h->cfg = *cfg;
+    if (cfg->precision == SW2D_FP32) {
+        h->R = cfg->rows;
+        h->C = cfg->cols;
+        const size_t need = sw2d::Engine32::scenario_bytes(cfg->rows, cfg->cols, false, 0);
+        if (cfg->hbm_budget_bytes > 0 && (double)need > cfg->hbm_budget_bytes) {
+            delete h;
+            return fail(SW2D_ERR_BUDGET, "model does not fit the HBM budget");
+        }
+        h->eng.reset(new sw2d::Engine32(cfg->device));
+        std::string err;
+        int rc0 = h->eng->init(&err);
+        if (rc0) {
+            delete h;
+            return fail(rc0, err);
+        }
+        h->in_rain.assign(1, 0.0);
+        *out = h;
+        return SW2D_OK;
+    }
     h->R = cfg->rows;
     h->C = cfg->cols;
     h->P = ((cfg->cols + 2 * SW2D_HALO + 31) / 32) * 32;
@@ -446,7 +551,8 @@ int sw2d_create(const sw2d_config* cfg, sw2d_handle** out) {
     TRY(dalloc(&h->uu1, h->ncell));
     TRY(dalloc(&h->vv1, h->ncell));
     TRY(dalloc(&h->drys, h->ncell));
-    TRY(dalloc(&h->partials, (size_t)h->params().nblocks_cells * 8 + 8));
+    TRY(dalloc(&h->partials, (size_t)h->params().nblocks_cells * 4 + 8));
+    TRY(dalloc(&h->partials_f, (size_t)h->params().nblocks_faces * 2 + 8));
     TRY(dalloc(&h->clk, 1));
     TRY(dalloc(&h->rain, 4));
     TRY(dalloc(&h->srcq, 4));
@@ -472,6 +578,11 @@ int sw2d_create(const sw2d_config* cfg, sw2d_handle** out) {
 
 int sw2d_destroy(sw2d_handle* h) {
     if (!h) return SW2D_OK;
+    if (h->fp32()) {
+        h->eng.reset();
+        delete h;
+        return SW2D_OK;
+    }
     cudaSetDevice(h->cfg.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->graph) cudaGraphExecDestroy(h->graph);
@@ -493,6 +604,7 @@ int sw2d_destroy(sw2d_handle* h) {
     dfree(h->evap);
     dfree(h->srcq);
     dfree(h->partials);
+    dfree(h->partials_f);
     dfree(h->outlet);
     dfree(h->clk);
     dfree(h->scratch);
@@ -510,6 +622,11 @@ int sw2d_destroy(sw2d_handle* h) {
 
 int sw2d_set_dem(sw2d_handle* h, const double* zin) {
     if (!h || !zin) return fail(SW2D_ERR_INVALID, "null argument");
+    if (h->fp32()) {
+        h->in_dem.assign(zin, zin + (size_t)h->R * h->C);
+        h->have_dem = true;
+        return SW2D_OK;
+    }
     int rc = set_device(h);
     if (rc) return rc;
     if ((rc = upload_interior(h, h->z, zin, h->R, h->C))) return rc;
@@ -532,6 +649,11 @@ int sw2d_set_dem(sw2d_handle* h, const double* zin) {
 int sw2d_set_depth(sw2d_handle* h, const double* d) {
     if (!h || !d) return fail(SW2D_ERR_INVALID, "null argument");
     if (!h->have_dem) return fail(SW2D_ERR_STATE, "set_dem first");
+    if (h->fp32()) {
+        h->in_depth.assign(d, d + (size_t)h->R * h->C);
+        h->have_depth = true;
+        return fp32_rebuild(h);
+    }
     int rc = set_device(h);
     if (rc) return rc;
     std::vector<double> dd(d, d + (size_t)h->R * h->C);
@@ -557,6 +679,19 @@ int sw2d_set_depth(sw2d_handle* h, const double* d) {
 
 int sw2d_set_manning_classes(sw2d_handle* h, const uint8_t* cls, const double* table, int ntable) {
     if (!h) return fail(SW2D_ERR_INVALID, "null handle");
+    if (h->fp32()) {
+        if (!cls) {
+            h->in_mcls.clear();
+            h->in_mtab.clear();
+        } else {
+            if (!table || ntable <= 0 || ntable > 64) return fail(SW2D_ERR_INVALID, "manning table (FP32: <= 64 classes)");
+            for (size_t k = 0; k < (size_t)h->R * h->C; k++)
+                if (cls[k] >= ntable) return fail(SW2D_ERR_INVALID, "manning class out of table range");
+            h->in_mcls.assign(cls, cls + (size_t)h->R * h->C);
+            h->in_mtab.assign(table, table + ntable);
+        }
+        return h->have_depth ? fp32_rebuild(h) : SW2D_OK;
+    }
     int rc = set_device(h);
     if (rc) return rc;
     if (!cls) {
@@ -579,6 +714,12 @@ int sw2d_set_manning_classes(sw2d_handle* h, const uint8_t* cls, const double* t
 
 int sw2d_set_rain_series(sw2d_handle* h, const double* mm, int n, double dtrain) {
     if (!h || (n > 0 && !mm) || n < 0 || !(dtrain > 0)) return fail(SW2D_ERR_INVALID, "rain series");
+    if (h->fp32()) {
+        h->in_rain.assign(mm, mm + n);
+        if (n == 0) h->in_rain.assign(1, 0.0);
+        h->dtrain = dtrain;
+        return h->have_depth ? fp32_rebuild(h) : SW2D_OK;
+    }
     int rc = set_device(h);
     if (rc) return rc;
     std::vector<double> v(n + 2, 0.0);
@@ -594,6 +735,11 @@ int sw2d_set_rain_series(sw2d_handle* h, const double* mm, int n, double dtrain)
 
 int sw2d_set_rain_field(sw2d_handle* h, const float* w) {
     if (!h) return fail(SW2D_ERR_INVALID, "null handle");
+    if (h->fp32()) {
+        if (w) h->in_rainw.assign(w, w + (size_t)h->R * h->C);
+        else h->in_rainw.clear();
+        return h->have_depth ? fp32_rebuild(h) : SW2D_OK;
+    }
     int rc = set_device(h);
     if (rc) return rc;
     if (!w) {
@@ -611,6 +757,7 @@ int sw2d_set_rain_field(sw2d_handle* h, const float* w) {
 
 int sw2d_set_evaporation_series(sw2d_handle* h, const double* mm, int n) {
     if (!h || n < 0 || (n > 0 && !mm)) return fail(SW2D_ERR_INVALID, "evaporation series");
+    if (h->fp32()) return fail(SW2D_ERR_STATE, "evaporation series: FP64 precision only");
     int rc = set_device(h);
     if (rc) return rc;
     dfree(h->evap);
@@ -627,6 +774,7 @@ int sw2d_set_evaporation_series(sw2d_handle* h, const double* mm, int n) {
 }
 
 int sw2d_set_point_sources(sw2d_handle* h, int nsrc, const int* cells, const double* q, int nq, double dtoq) {
+    if (h && h->fp32()) return fail(SW2D_ERR_STATE, "point sources: FP64 precision only");
     if (!h || nsrc < 0 || nsrc > SW2D_MAX_SRC || (nsrc > 0 && (!cells || !q || nq <= 0 || !(dtoq > 0))))
         return fail(SW2D_ERR_INVALID, "point sources");
     if (!h->have_dem) return fail(SW2D_ERR_STATE, "set_dem first");
@@ -668,7 +816,7 @@ int sw2d_advance(sw2d_handle* h, double t_end, int64_t* iterations_out) {
 int sw2d_step(sw2d_handle* h, int n, double t_end) {
     if (n < 0) return fail(SW2D_ERR_INVALID, "n < 0");
     int64_t done = 0;
-    if (h && h->cfg.dt_mode == SW2D_DT_CFL && (n & 1)) {
+    if (h && !h->fp32() && h->cfg.dt_mode == SW2D_DT_CFL && (n & 1)) {
         return fail(SW2D_ERR_INVALID, "CFL mode steps in pairs of iterations");
     }
     return run_until(h, t_end, n, &done);
@@ -678,6 +826,15 @@ int sw2d_get_time(sw2d_handle* h, double* t, int64_t* iters) {
     if (!h) return fail(SW2D_ERR_INVALID, "null handle");
     int rc = set_device(h);
     if (rc) return rc;
+    if (h->fp32()) {
+        if (h->eng_idx < 0) return fail(SW2D_ERR_STATE, "set_depth first");
+        sw2d::Clock32 c;
+        std::string err;
+        if ((rc = h->eng->get_clock(h->eng_idx, &c, &err))) return fail(rc, err);
+        if (t) *t = c.t;
+        if (iters) *iters = c.iters;
+        return SW2D_OK;
+    }
     DevClock c;
     if ((rc = read_clock(h, &c))) return rc;
     if (t) *t = c.t;
@@ -688,15 +845,57 @@ int sw2d_get_time(sw2d_handle* h, double* t, int64_t* iters) {
 int sw2d_get_state(sw2d_handle* h, double* depth, double* qx, double* qy) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (h->fp32()) {
+        std::string err;
+        if ((rc = h->eng->get_state(h->eng_idx, depth, qx, qy, &err))) return fail(rc, err);
+        return SW2D_OK;
+    }
     if (depth && (rc = download_block(h, depth, h->h[0], 0, 0, h->R, h->C))) return rc;
     if (qx && (rc = download_block(h, qx, h->qx[0], 0, 0, h->R + 1, h->C))) return rc;
     if (qy && (rc = download_block(h, qy, h->qy[0], 0, 0, h->R, h->C + 1))) return rc;
     return SW2D_OK;
 }
 
+/* FP32 handles: the reference's uu1_vv1 / uu_vv / uua_vva formulas
+ * (SW2D-EFDC.cu:404-522) applied to the downloaded state, for output. */
+static int velocities_fp32(sw2d_handle* h, double* uu, double* vv, double* uua, double* vva) {
+    const int R = h->R, C = h->C;
+    std::vector<double> d((size_t)R * C), qx((size_t)(R + 1) * C), qy((size_t)R * (C + 1));
+    std::string err;
+    int rc = h->eng->get_state(h->eng_idx, d.data(), qx.data(), qy.data(), &err);
+    if (rc) return fail(rc, err);
+    const double th = h->cfg.th;
+    std::vector<double> u1((size_t)(R + 1) * C, 0.0), v1((size_t)R * (C + 1), 0.0);
+    for (int r = 0; r <= R; r++)
+        for (int c = 0; c < C; c++) {
+            double hm = r == 0 ? d[c] : (r == R ? d[(size_t)(R - 1) * C + c] : 0.5 * (d[(size_t)r * C + c] + d[(size_t)(r - 1) * C + c]));
+            double q = qx[(size_t)r * C + c];
+            u1[(size_t)r * C + c] = hm >= th ? q / hm : 0.0;
+        }
+    for (int r = 0; r < R; r++)
+        for (int c = 0; c <= C; c++) {
+            double hn = c == 0 ? d[(size_t)r * C] : (c == C ? d[(size_t)r * C + C - 1] : 0.5 * (d[(size_t)r * C + c] + d[(size_t)r * C + c - 1]));
+            double q = qy[(size_t)r * (C + 1) + c];
+            v1[(size_t)r * (C + 1) + c] = hn >= th ? q / hn : 0.0;
+        }
+    auto U = [&](int r, int c) { return u1[(size_t)r * C + c]; };
+    auto V = [&](int r, int c) { return v1[(size_t)r * (C + 1) + c]; };
+    for (int r = 0; r < R; r++)
+        for (int c = 0; c < C; c++) {
+            const size_t k = (size_t)r * C + c;
+            const bool wet = d[k] >= th;
+            if (uu) uu[k] = wet ? (U(r + 1, c) + U(r, c)) / 2.00 : 0.0;
+            if (vv) vv[k] = wet ? (V(r, c + 1) + V(r, c)) / 2.00 : 0.0;
+            if (uua) uua[k] = c > 0 ? 0.250 * (U(r, c) + U(r + 1, c) + U(r, c - 1) + U(r + 1, c - 1)) : 0.50 * (U(r, c) + U(r + 1, c));
+            if (vva) vva[k] = r > 0 ? 0.250 * (V(r, c) + V(r, c + 1) + V(r - 1, c) + V(r - 1, c + 1)) : 0.50 * (V(r, c) + V(r, c + 1));
+        }
+    return SW2D_OK;
+}
+
 static int velocities(sw2d_handle* h, double* uu, double* vv, double* uua, double* vva) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (h->fp32()) return velocities_fp32(h, uu, vv, uua, vva);
     const size_t n = (size_t)h->R * h->C;
     if (!h->scratch && (rc = dalloc(&h->scratch, 4 * n))) return rc;
     StepParams p = h->params();
@@ -719,6 +918,30 @@ int sw2d_get_ledger(sw2d_handle* h, sw2d_ledger* out) {
     if (!h || !out) return fail(SW2D_ERR_INVALID, "null argument");
     int rc = set_device(h);
     if (rc) return rc;
+    if (h->fp32()) {
+        if (h->eng_idx < 0) return fail(SW2D_ERR_STATE, "set_depth first");
+        sw2d::Clock32 c;
+        std::string err;
+        double vol = 0, smax = 0;
+        if ((rc = h->eng->get_clock(h->eng_idx, &c, &err))) return fail(rc, err);
+        if ((rc = h->eng->get_volume(h->eng_idx, &vol, &smax, &err))) return fail(rc, err);
+        out->time = c.t;
+        out->iterations = (double)c.iters;
+        out->volume = vol;
+        out->volume0 = c.volume0;
+        out->rain_in = c.rain_in;
+        out->source_in = c.source_in;
+        out->evap_out = c.evap_out;
+        out->outflow = c.outflow;
+        out->clamp_gain = c.clamp_gain;
+        out->q_out = c.q_out;
+        out->s_max = c.s_max;
+        out->dt_last = c.dt2;
+        double inflow = out->rain_in + out->source_in;
+        double resid = out->volume - out->volume0 - out->rain_in - out->source_in + out->evap_out + out->outflow;
+        out->balance_error = resid / std::max(std::fabs(inflow), 1e-300);
+        return SW2D_OK;
+    }
     if (h->have_depth && (rc = prime(h, 1))) return rc; /* volume of the current state */
     DevClock c;
     if ((rc = read_clock(h, &c))) return rc;
@@ -744,6 +967,10 @@ int sw2d_set_outlet_record(sw2d_handle* h, int capacity) {
     if (!h || capacity < 0) return fail(SW2D_ERR_INVALID, "capacity");
     int rc = set_device(h);
     if (rc) return rc;
+    if (h->fp32()) {
+        h->outlet_cap = capacity;
+        return h->have_depth ? fp32_rebuild(h) : SW2D_OK;
+    }
     dfree(h->outlet);
     h->outlet_cap = 0;
     if (capacity > 0) {
@@ -760,6 +987,12 @@ int sw2d_get_outlet(sw2d_handle* h, double* t, double* q, int capacity, int* cou
     if (!h) return fail(SW2D_ERR_INVALID, "null handle");
     int rc = set_device(h);
     if (rc) return rc;
+    if (h->fp32()) {
+        if (h->eng_idx < 0) return fail(SW2D_ERR_STATE, "set_depth first");
+        std::string err;
+        if ((rc = h->eng->get_outlet(h->eng_idx, t, q, capacity, count_out, &err))) return fail(rc, err);
+        return SW2D_OK;
+    }
     DevClock c;
     if ((rc = read_clock(h, &c))) return rc;
     long long n = std::min<long long>(c.outlet_n, h->outlet_cap);
@@ -786,6 +1019,11 @@ int sw2d_set_profiling(sw2d_handle* h, int on) {
 
 int sw2d_get_timing(sw2d_handle* h, double* ms, double* kernel_ms, int* nk) {
     if (!h) return fail(SW2D_ERR_INVALID, "null handle");
+    if (h->fp32()) {
+        if (ms) *ms = h->last_ms_per_iter;
+        if (nk) *nk = 0;
+        return SW2D_OK;
+    }
     if (ms) *ms = h->last_ms_per_iter;
     const int n = fp64_kernels_per_iteration();
     if (nk) *nk = n;
@@ -796,6 +1034,7 @@ int sw2d_get_timing(sw2d_handle* h, double* ms, double* kernel_ms, int* nk) {
 
 int sw2d_snapshot_size(sw2d_handle* h, size_t* bytes) {
     if (!h || !bytes) return fail(SW2D_ERR_INVALID, "null argument");
+    if (h->fp32()) return fail(SW2D_ERR_STATE, "snapshot: FP64 precision only");
     *bytes = 64 + sizeof(DevClock) + 3 * h->ncell * sizeof(double);
     return SW2D_OK;
 }
@@ -803,6 +1042,7 @@ int sw2d_snapshot_size(sw2d_handle* h, size_t* bytes) {
 int sw2d_snapshot(sw2d_handle* h, void* buf, size_t bytes) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (h->fp32()) return fail(SW2D_ERR_STATE, "snapshot: FP64 precision only");
     size_t need;
     sw2d_snapshot_size(h, &need);
     if (!buf || bytes < need) return fail(SW2D_ERR_INVALID, "snapshot buffer too small");
@@ -822,6 +1062,7 @@ int sw2d_snapshot(sw2d_handle* h, void* buf, size_t bytes) {
 
 int sw2d_restore(sw2d_handle* h, const void* buf, size_t bytes) {
     if (!h || !buf) return fail(SW2D_ERR_INVALID, "null argument");
+    if (h->fp32()) return fail(SW2D_ERR_STATE, "restore: FP64 precision only");
     if (!h->have_dem) return fail(SW2D_ERR_STATE, "set_dem first");
     int rc = set_device(h);
     if (rc) return rc;
@@ -857,6 +1098,7 @@ int sw2d_restore(sw2d_handle* h, const void* buf, size_t bytes) {
 
 int sw2d_set_coupling_mask(sw2d_handle* h, const int* mask, int lagged, int* n_faces_out) {
     if (!h || !mask) return fail(SW2D_ERR_INVALID, "null argument");
+    if (h->fp32()) return fail(SW2D_ERR_STATE, "coupling: FP64 precision only");
     int rc = set_device(h);
     if (rc) return rc;
     const int rows = h->R, cols = h->C;

@@ -1,0 +1,471 @@
+/* Host engine of the FP32 precision form (see sw2d_engine.h). */
+#include "sw2d_engine.h"
+
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace sw2d {
+
+namespace {
+
+constexpr int kChunk32 = 16; /* iterations per captured graph */
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+bool make_map(CUtensorMap* tm, void* base, CUtensorMapDataType dt, size_t esize, uint64_t width, uint64_t height,
+              uint32_t boxw, uint32_t boxh) {
+    auto fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {width, height};
+    cuuint64_t strides[1] = {width * esize};
+    cuuint32_t box[2] = {boxw, boxh};
+    cuuint32_t es[2] = {1, 1};
+    return fn(tm, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int pitch_of(int cols) { return ((cols + 2 * T32_H + 31) / 32) * 32; }
+
+#define ECK(call)                                                                   \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            if (err) *err = std::string(#call) + ": " + cudaGetErrorString(e_);     \
+            return e_ == cudaErrorMemoryAllocation ? SW2D_ERR_NOMEM : SW2D_ERR_CUDA; \
+        }                                                                           \
+    } while (0)
+
+} // namespace
+
+Engine32::Engine32(int device) : device_(device) {}
+
+Engine32::~Engine32() {
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (auto& s : scn_)
+        for (void* p : s->allocs) cudaFree(p);
+    if (graph_) cudaGraphExecDestroy(graph_);
+    cudaFree(d_scn_);
+    cudaFree(d_work_);
+    cudaFree(d_part_);
+    cudaFree(d_tmp_);
+    if (ev_a_) cudaEventDestroy(ev_a_);
+    if (ev_b_) cudaEventDestroy(ev_b_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+int Engine32::init(std::string* err) {
+    ECK(cudaSetDevice(device_));
+    ECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    ECK(cudaEventCreate(&ev_a_));
+    ECK(cudaEventCreate(&ev_b_));
+    ECK(cudaMalloc(&d_tmp_, 4 * sizeof(double)));
+    if (fp32_configure_kernels() != 0) {
+        if (err) *err = "cannot enable the FP32 kernel's shared memory";
+        return SW2D_ERR_CUDA;
+    }
+    if (!encode_fn()) {
+        if (err) *err = "cuTensorMapEncodeTiled unavailable";
+        return SW2D_ERR_CUDA;
+    }
+    return SW2D_OK;
+}
+
+size_t Engine32::scenario_bytes(int rows, int cols, bool rain_field, int outlet_cap) {
+    const size_t P = pitch_of(cols), NR = rows + 2 * T32_H;
+    const size_t cells = P * NR;
+    size_t b = cells * (8 * sizeof(float) + 1);
+    if (rain_field) b += cells * sizeof(float);
+    const size_t tiles = (size_t)((cols + T32_TC - 1) / T32_TC) * ((rows + T32_TR - 1) / T32_TR);
+    b += tiles * sizeof(float) + (size_t)outlet_cap * 16 + sizeof(Clock32) + 4096;
+    return b;
+}
+
+size_t Engine32::bytes_in_use() const {
+    size_t b = 0;
+    for (auto& s : scn_) b += s->bytes;
+    return b;
+}
+
+int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* index_out) {
+    ECK(cudaSetDevice(device_));
+    if (in.rows < 2 || in.cols < 2 || !in.dem) {
+        if (err) *err = "scenario needs rows, cols >= 2 and a DEM";
+        return SW2D_ERR_INVALID;
+    }
+    if (in.mclass && (in.ntable <= 0 || in.ntable > T32_MAXCLASS || !in.mtable)) {
+        if (err) *err = "Manning table must have 1..64 entries";
+        return SW2D_ERR_INVALID;
+    }
+    auto sp = std::make_unique<Scenario32>();
+    Scenario32& S = *sp;
+    S.id = id;
+    const int R = in.rows, C = in.cols, P = pitch_of(C), NR = R + 2 * T32_H;
+    S.R = R;
+    S.C = C;
+    S.P = P;
+    S.NR = NR;
+    const size_t cells = (size_t)P * NR;
+    const int tx = (C + T32_TC - 1) / T32_TC, ty = (R + T32_TR - 1) / T32_TR;
+    auto alloc = [&](size_t bytes, void** p) -> int {
+        cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess) {
+            if (err) *err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+            return SW2D_ERR_NOMEM;
+        }
+        S.allocs.push_back(*p);
+        S.bytes += bytes;
+        cudaMemsetAsync(*p, 0, std::max<size_t>(bytes, 16), stream_);
+        return SW2D_OK;
+    };
+    auto fail_free = [&](int rc) {
+        cudaStreamSynchronize(stream_);
+        for (void* p : S.allocs) cudaFree(p);
+        return rc;
+    };
+    Scn32& d = S.d;
+    void* p;
+    int rc;
+    for (int k = 0; k < 2; k++) {
+        if ((rc = alloc(cells * 4, &p))) return fail_free(rc);
+        d.h[k] = (float*)p;
+        if ((rc = alloc(cells * 4, &p))) return fail_free(rc);
+        d.qx[k] = (float*)p;
+        if ((rc = alloc(cells * 4, &p))) return fail_free(rc);
+        d.qy[k] = (float*)p;
+    }
+    if ((rc = alloc(cells * 4, &p))) return fail_free(rc);
+    d.kc = (float*)p;
+    float* dz;
+    if ((rc = alloc(cells * 4, &p))) return fail_free(rc);
+    dz = (float*)p;
+    uint8_t* dinfo;
+    if ((rc = alloc(cells, &p))) return fail_free(rc);
+    dinfo = (uint8_t*)p;
+    d.info = dinfo;
+    float* ddatum;
+    if ((rc = alloc((size_t)tx * ty * 4, &p))) return fail_free(rc);
+    ddatum = (float*)p;
+    d.datum = ddatum;
+    float* drw = nullptr;
+    if (in.rain_weight) {
+        if ((rc = alloc(cells * 4, &p))) return fail_free(rc);
+        drw = (float*)p;
+    }
+    d.rainw = drw;
+    const int nrain = std::max(in.nrain, 1);
+    double* drain;
+    if ((rc = alloc((size_t)(nrain + 2) * 8, &p))) return fail_free(rc);
+    drain = (double*)p;
+    d.rain = drain;
+    d.evap = nullptr;
+    d.outlet = nullptr;
+    if (in.outlet_cap > 0) {
+        if ((rc = alloc((size_t)in.outlet_cap * 16, &p))) return fail_free(rc);
+        d.outlet = (double*)p;
+    }
+    Clock32* dclk;
+    if ((rc = alloc(sizeof(Clock32), &p))) return fail_free(rc);
+    dclk = (Clock32*)p;
+    d.clk = dclk;
+
+    /* host staging: per-tile datum (multiple of 1/16 m), bed offsets, info */
+    std::vector<float> datum((size_t)tx * ty, 0.f);
+    std::vector<float> zoff(cells, 0.f), hbuf(cells, 0.f), rw;
+    std::vector<uint8_t> info(cells, 0);
+    double active_weight = 0.0;
+    for (int j = 0; j < ty; j++)
+        for (int i = 0; i < tx; i++) {
+            double sum = 0;
+            long n = 0;
+            for (int r = j * T32_TR; r < std::min(R, (j + 1) * T32_TR); r++)
+                for (int c = i * T32_TC; c < std::min(C, (i + 1) * T32_TC); c++) {
+                    double z = in.dem[(size_t)r * C + c];
+                    if (z != in.nodata) {
+                        sum += z;
+                        n++;
+                    }
+                }
+            datum[(size_t)j * tx + i] = n ? (float)(std::round(sum / n * 16.0) / 16.0) : 0.f;
+        }
+    if (in.rain_weight) rw.assign(cells, 0.f);
+    for (int r = 0; r < R; r++)
+        for (int c = 0; c < C; c++) {
+            const size_t k = (size_t)r * C + c;
+            const size_t g = (size_t)(r + T32_H) * P + (c + T32_H);
+            const double z = in.dem[k];
+            const bool act = z != in.nodata;
+            const double dat = datum[(size_t)(r / T32_TR) * tx + (c / T32_TC)];
+            zoff[g] = act ? (float)(z - dat) : 0.f;
+            uint8_t cls = in.mclass ? in.mclass[k] : 0;
+            if (in.mclass && cls >= in.ntable) {
+                if (err) *err = "Manning class out of table range";
+                return fail_free(SW2D_ERR_INVALID);
+            }
+            info[g] = (uint8_t)((act ? SW2D_I_ACTIVE : 0) | (cls << 1));
+            hbuf[g] = (act && in.depth) ? (float)in.depth[k] : 0.f;
+            if (in.rain_weight) rw[g] = in.rain_weight[k];
+            if (act) active_weight += in.rain_weight ? (double)in.rain_weight[k] : 1.0;
+        }
+    ECK(cudaMemcpyAsync(dz, zoff.data(), cells * 4, cudaMemcpyHostToDevice, stream_));
+    ECK(cudaMemcpyAsync(dinfo, info.data(), cells, cudaMemcpyHostToDevice, stream_));
+    ECK(cudaMemcpyAsync(d.h[0], hbuf.data(), cells * 4, cudaMemcpyHostToDevice, stream_));
+    ECK(cudaMemcpyAsync(ddatum, datum.data(), datum.size() * 4, cudaMemcpyHostToDevice, stream_));
+    if (drw) ECK(cudaMemcpyAsync(drw, rw.data(), cells * 4, cudaMemcpyHostToDevice, stream_));
+    std::vector<double> rain(nrain + 2, 0.0);
+    for (int k = 0; k < in.nrain; k++) rain[k] = in.rain[k];
+    ECK(cudaMemcpyAsync(drain, rain.data(), rain.size() * 8, cudaMemcpyHostToDevice, stream_));
+
+    /* tensor maps: fields staged as 72 x 40 tiles, the info byte as 80 x 40 */
+    bool ok = true;
+    for (int k = 0; k < 2; k++) {
+        ok &= make_map(&d.tm_h[k], d.h[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, T32_LW, T32_LH);
+        ok &= make_map(&d.tm_qx[k], d.qx[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, T32_LW, T32_LH);
+        ok &= make_map(&d.tm_qy[k], d.qy[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, T32_LW, T32_LH);
+    }
+    ok &= make_map(&d.tm_z, dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, T32_LW, T32_LH);
+    ok &= make_map(&d.tm_info, dinfo, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P, NR, T32_LWB, T32_LH);
+    if (!ok) {
+        if (err) *err = "cuTensorMapEncodeTiled failed";
+        return fail_free(SW2D_ERR_CUDA);
+    }
+    d.R = R;
+    d.C = C;
+    d.P = P;
+    d.tiles_x = tx;
+    d.tiles_y = ty;
+    d.outflow_south = in.outflow_south;
+    d.series_mode = in.series_mode;
+    d.dt_mode = in.dt_mode;
+    d.nrain = nrain;
+    d.nevap = 0;
+    d.outlet_cap = in.outlet_cap;
+    d.dx = (float)in.dx;
+    d.dy = (float)in.dy;
+    d.rdx = (float)(1.0 / in.dx);
+    d.rdy = (float)(1.0 / in.dy);
+    d.th = (float)in.th;
+    d.g = (float)in.g;
+    const double pct_lake = 1.00 - in.frac_lwl, pct_land = 1.00 - (in.frac_int + in.frac_inf);
+    d.pct_lake = (float)pct_lake;
+    d.pct_land = (float)pct_land;
+    d.ev_wl_min = (float)in.ev_wl_min;
+    d.ledger_cells = pct_lake != pct_land;
+    d.rain_static = active_weight * pct_land;
+    d.dxd = in.dx;
+    d.dyd = in.dy;
+    d.dtrain = in.dtrain;
+    d.dt_fixed = in.dt;
+    d.cfl = in.cfl;
+    d.dt_max = in.dt_max;
+    d.area = in.dx * in.dy;
+    for (int k = 0; k < T32_MAXCLASS; k++)
+        d.ntab[k] = (float)(in.mclass ? (k < in.ntable ? in.mtable[k] : 0.0) : in.manning);
+    Clock32 c{};
+    c.t = in.t0;
+    c.t_end = in.t_end;
+    ECK(cudaMemcpyAsync(dclk, &c, sizeof c, cudaMemcpyHostToDevice, stream_));
+    ECK(cudaStreamSynchronize(stream_));
+    S.t_end_default = in.t_end;
+    scn_.push_back(std::move(sp));
+    const int idx = (int)scn_.size() - 1;
+    dirty_ = true;
+    if ((rc = rebuild(err))) return rc;
+    /* initial volume and CFL speed, then the first slot */
+    fp32_launch_volume(d_scn_, idx, scn_[idx]->d, d_tmp_, stream_);
+    double vs[2];
+    ECK(cudaMemcpyAsync(vs, d_tmp_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    ECK(cudaStreamSynchronize(stream_));
+    c.volume0 = vs[0];
+    c.s_max = vs[1];
+    ECK(cudaMemcpyAsync(dclk, &c, sizeof c, cudaMemcpyHostToDevice, stream_));
+    fp32_launch_prime(d_scn_ + idx, 1, stream_);
+    ECK(cudaStreamSynchronize(stream_));
+    ECK(cudaGetLastError());
+    if (index_out) *index_out = idx;
+    return SW2D_OK;
+}
+
+int Engine32::remove(int index) {
+    if (index < 0 || index >= (int)scn_.size()) return SW2D_ERR_INVALID;
+    cudaSetDevice(device_);
+    cudaStreamSynchronize(stream_);
+    for (void* p : scn_[index]->allocs) cudaFree(p);
+    scn_.erase(scn_.begin() + index);
+    dirty_ = true;
+    return SW2D_OK;
+}
+
+int Engine32::rebuild(std::string* err) {
+    if (!dirty_) return SW2D_OK;
+    work_.clear();
+    std::vector<Scn32> host(scn_.size());
+    for (size_t i = 0; i < scn_.size(); i++) {
+        Scn32& d = scn_[i]->d;
+        d.first_work = (int)work_.size();
+        for (int ty = 0; ty < d.tiles_y; ty++)
+            for (int tx = 0; tx < d.tiles_x; tx++) work_.push_back(make_int4((int)i, tx, ty, 0));
+        d.nwork = (int)work_.size() - d.first_work;
+        host[i] = d;
+    }
+    if (host.size() > d_scn_cap_) {
+        cudaFree(d_scn_);
+        d_scn_ = nullptr;
+        d_scn_cap_ = std::max<size_t>(host.size(), 2 * d_scn_cap_);
+        ECK(cudaMalloc(&d_scn_, d_scn_cap_ * sizeof(Scn32)));
+    }
+    if (work_.size() > d_work_cap_) {
+        cudaFree(d_work_);
+        cudaFree(d_part_);
+        d_work_ = nullptr;
+        d_part_ = nullptr;
+        d_work_cap_ = std::max<size_t>(work_.size(), 2 * d_work_cap_);
+        ECK(cudaMalloc(&d_work_, d_work_cap_ * sizeof(int4)));
+        ECK(cudaMalloc(&d_part_, d_work_cap_ * sizeof(Part32)));
+    }
+    if (!host.empty())
+        ECK(cudaMemcpyAsync(d_scn_, host.data(), host.size() * sizeof(Scn32), cudaMemcpyHostToDevice, stream_));
+    if (!work_.empty())
+        ECK(cudaMemcpyAsync(d_work_, work_.data(), work_.size() * sizeof(int4), cudaMemcpyHostToDevice, stream_));
+    ECK(cudaStreamSynchronize(stream_));
+    if (graph_) {
+        cudaGraphExecDestroy(graph_);
+        graph_ = nullptr;
+    }
+    dirty_ = false;
+    return SW2D_OK;
+}
+
+int Engine32::build_graph(std::string* err) {
+    if (graph_) return SW2D_OK;
+    cudaGraph_t g;
+    ECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < kChunk32; k++)
+        fp32_launch_iteration(d_scn_, (int)scn_.size(), d_work_, (int)work_.size(), d_part_, stream_);
+    ECK(cudaStreamEndCapture(stream_, &g));
+    cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        if (err) *err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e);
+        return SW2D_ERR_CUDA;
+    }
+    return SW2D_OK;
+}
+
+int Engine32::set_t_end(int index, double t_end, std::string* err) {
+    ECK(cudaSetDevice(device_));
+    for (int i = 0; i < (int)scn_.size(); i++) {
+        if (index >= 0 && i != index) continue;
+        ECK(cudaMemcpyAsync(&scn_[i]->d.clk->t_end, &t_end, sizeof(double), cudaMemcpyHostToDevice, stream_));
+        ECK(cudaStreamSynchronize(stream_));
+    }
+    int rc = rebuild(err);
+    if (rc) return rc;
+    if (index >= 0)
+        fp32_launch_prime(d_scn_ + index, 1, stream_);
+    else if (!scn_.empty())
+        fp32_launch_prime(d_scn_, (int)scn_.size(), stream_);
+    ECK(cudaStreamSynchronize(stream_));
+    return SW2D_OK;
+}
+
+int Engine32::run(long long n, std::string* err) {
+    ECK(cudaSetDevice(device_));
+    int rc = rebuild(err);
+    if (rc) return rc;
+    if (scn_.empty() || n <= 0) return SW2D_OK;
+    if ((rc = build_graph(err))) return rc;
+    ECK(cudaEventRecord(ev_a_, stream_));
+    for (long long k = 0; k < n / kChunk32; k++) ECK(cudaGraphLaunch(graph_, stream_));
+    for (long long k = 0; k < n % kChunk32; k++)
+        fp32_launch_iteration(d_scn_, (int)scn_.size(), d_work_, (int)work_.size(), d_part_, stream_);
+    ECK(cudaGetLastError());
+    ECK(cudaEventRecord(ev_b_, stream_));
+    ECK(cudaEventSynchronize(ev_b_));
+    float ms = 0;
+    ECK(cudaEventElapsedTime(&ms, ev_a_, ev_b_));
+    last_ms_ = ms;
+    last_iters_ = n;
+    return SW2D_OK;
+}
+
+int Engine32::sync(std::string* err) {
+    ECK(cudaStreamSynchronize(stream_));
+    return SW2D_OK;
+}
+
+int Engine32::get_clock(int index, Clock32* out, std::string* err) {
+    ECK(cudaMemcpyAsync(out, scn_[index]->d.clk, sizeof(Clock32), cudaMemcpyDeviceToHost, stream_));
+    ECK(cudaStreamSynchronize(stream_));
+    return SW2D_OK;
+}
+
+int Engine32::get_state(int index, double* depth, double* qx, double* qy, std::string* err) {
+    Scenario32& S = *scn_[index];
+    Clock32 c;
+    int rc = get_clock(index, &c, err);
+    if (rc) return rc;
+    const int cur = c.slot.cur;
+    const int R = S.R, C = S.C, P = S.P;
+    std::vector<float> buf((size_t)(R + 1) * (C + 1));
+    auto fetch = [&](const float* src, int rows, int cols, double* dst) -> int {
+        ECK(cudaMemcpy2DAsync(buf.data(), (size_t)cols * 4, src + (size_t)T32_H * P + T32_H, (size_t)P * 4,
+                              (size_t)cols * 4, rows, cudaMemcpyDeviceToHost, stream_));
+        ECK(cudaStreamSynchronize(stream_));
+        for (size_t k = 0; k < (size_t)rows * cols; k++) dst[k] = buf[k];
+        return SW2D_OK;
+    };
+    if (depth && (rc = fetch(S.d.h[cur], R, C, depth))) return rc;
+    if (qx && (rc = fetch(S.d.qx[cur], R + 1, C, qx))) return rc;
+    if (qy && (rc = fetch(S.d.qy[cur], R, C + 1, qy))) return rc;
+    return SW2D_OK;
+}
+
+int Engine32::get_volume(int index, double* vol, double* smax, std::string* err) {
+    int rc = rebuild(err);
+    if (rc) return rc;
+    fp32_launch_volume(d_scn_, index, scn_[index]->d, d_tmp_, stream_);
+    double vs[2];
+    ECK(cudaMemcpyAsync(vs, d_tmp_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    ECK(cudaStreamSynchronize(stream_));
+    if (vol) *vol = vs[0];
+    if (smax) *smax = vs[1];
+    return SW2D_OK;
+}
+
+int Engine32::get_outlet(int index, double* t, double* q, int cap, int* count, std::string* err) {
+    Scenario32& S = *scn_[index];
+    Clock32 c;
+    int rc = get_clock(index, &c, err);
+    if (rc) return rc;
+    const int oc = S.d.outlet_cap;
+    long long n = std::min<long long>(c.outlet_n, oc);
+    if (count) *count = (int)n;
+    if (!n || (!t && !q)) return SW2D_OK;
+    std::vector<double> buf((size_t)oc * 2);
+    ECK(cudaMemcpyAsync(buf.data(), S.d.outlet, buf.size() * 8, cudaMemcpyDeviceToHost, stream_));
+    ECK(cudaStreamSynchronize(stream_));
+    long long first = c.outlet_n > oc ? c.outlet_n % oc : 0;
+    for (long long k = 0; k < n && k < cap; k++) {
+        long long j = (first + k) % oc;
+        if (t) t[k] = buf[2 * j];
+        if (q) q[k] = buf[2 * j + 1];
+    }
+    return SW2D_OK;
+}
+
+} // namespace sw2d

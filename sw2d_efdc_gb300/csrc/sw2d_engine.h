@@ -1,0 +1,94 @@
+/* Host engine of the FP32 precision form: owns the scenarios that one fused
+ * kernel launch advances together (one scenario for a single raster, many
+ * for the batched and served forms). */
+#ifndef SW2D_ENGINE_H
+#define SW2D_ENGINE_H
+
+#include "sw2d.h"
+#include "sw2d_fp32.h"
+
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace sw2d {
+
+struct ScenarioInput {
+    int rows = 0, cols = 0;
+    double dx = 1, dy = 1, nodata = -9999.0, th = 1e-4, g = 9.80, manning = 0.03;
+    int dt_mode = 1, series_mode = 2, outflow_south = 0;
+    double dt = 0.04, cfl = 0.7, dt_max = 2.0, t0 = 0.0, t_end = 0.0;
+    double frac_int = 0, frac_inf = 0, frac_lwl = 0, ev_wl_min = 0.05;
+    const double* dem = nullptr;        /* rows*cols */
+    const double* depth = nullptr;      /* rows*cols or NULL (dry) */
+    const uint8_t* mclass = nullptr;    /* rows*cols or NULL */
+    const double* mtable = nullptr;
+    int ntable = 0;
+    const double* rain = nullptr;       /* mm per dtrain */
+    int nrain = 0;
+    double dtrain = 3600.0;
+    const float* rain_weight = nullptr; /* rows*cols or NULL */
+    int outlet_cap = 0;
+};
+
+struct Scenario32 {
+    Scn32 d{};                 /* host copy of the device descriptor */
+    int R = 0, C = 0, P = 0, NR = 0;
+    size_t bytes = 0;          /* device bytes held */
+    std::vector<void*> allocs;
+    double t_end_default = 0.0;
+    long long id = -1;
+    bool finished = false;
+};
+
+class Engine32 {
+  public:
+    explicit Engine32(int device);
+    ~Engine32();
+    int init(std::string* err);
+    /* device bytes a scenario of this size needs */
+    static size_t scenario_bytes(int rows, int cols, bool rain_field, int outlet_cap);
+    int add(const ScenarioInput& in, long long id, std::string* err, int* index_out);
+    int remove(int index);
+    int count() const { return (int)scn_.size(); }
+    Scenario32& at(int i) { return *scn_[i]; }
+    /* set every scenario's t_end (or one) and recompute first slots */
+    int set_t_end(int index, double t_end, std::string* err);
+    /* run n iterations of every scenario (finished ones idle) */
+    int run(long long n, std::string* err);
+    /* state of one scenario, reference orientation */
+    int get_state(int index, double* depth, double* qx, double* qy, std::string* err);
+    int get_clock(int index, Clock32* out, std::string* err);
+    int get_volume(int index, double* vol, double* smax, std::string* err);
+    int get_outlet(int index, double* t, double* q, int cap, int* count, std::string* err);
+    cudaStream_t stream() const { return stream_; }
+    size_t bytes_in_use() const;
+    double last_ms() const { return last_ms_; }
+    long long last_iters() const { return last_iters_; }
+    int nwork() const { return (int)work_.size(); }
+    int sync(std::string* err);
+
+  private:
+    int rebuild(std::string* err);
+    int build_graph(std::string* err);
+    int device_;
+    cudaStream_t stream_ = nullptr;
+    std::vector<std::unique_ptr<Scenario32>> scn_;
+    std::vector<int4> work_;
+    Scn32* d_scn_ = nullptr;
+    size_t d_scn_cap_ = 0;
+    int4* d_work_ = nullptr;
+    size_t d_work_cap_ = 0;
+    Part32* d_part_ = nullptr;
+    size_t d_part_cap_ = 0;
+    double* d_tmp_ = nullptr;
+    bool dirty_ = true;
+    cudaGraphExec_t graph_ = nullptr;
+    int graph_iters_ = 0;
+    cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr;
+    double last_ms_ = 0.0;
+    long long last_iters_ = 0;
+};
+
+} // namespace sw2d
+#endif

@@ -1,0 +1,100 @@
+/* FP32 precision form of the SW2D step: device-side structures shared by the
+ * fused tile kernel (sw2d_fp32.cu) and the scenario engine (sw2d_engine.cu).
+ *
+ * One kernel serves the single-raster, batched and served forms: its work
+ * list holds (scenario, tile) pairs and every scenario has its own
+ * descriptor, clock, iteration length and forcing.
+ *
+ * Layout of a scenario in HBM: binary32 fields with a 4-cell halo
+ * (rows + 8 rows of `pitch` floats, pitch a multiple of 32), cell (r, c) at
+ * (r + 4) * pitch + (c + 4).  The bed is stored as binary32 offsets from a
+ * per-tile datum (a multiple of 1/16 m, so datum differences are exact in
+ * binary32); the info byte holds the active bit and the Manning class.
+ */
+#ifndef SW2D_FP32_H
+#define SW2D_FP32_H
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace sw2d {
+
+constexpr int T32_TC = 64;  /* tile columns */
+constexpr int T32_TR = 32;  /* tile rows */
+constexpr int T32_H = 4;    /* halo */
+constexpr int T32_LW = T32_TC + 2 * T32_H; /* 72: staged tile width (floats) */
+constexpr int T32_LH = T32_TR + 2 * T32_H; /* 40: staged tile height */
+constexpr int T32_LWB = 80; /* staged byte-tile width (TMA inner extent multiple of 16 B) */
+constexpr int T32_NT = 256; /* threads per tile */
+constexpr int T32_MAXCLASS = 64;
+constexpr int T32_MAXSRC = 16;
+
+#define SW2D_I_ACTIVE 1u /* info bit 0; bits 1..6: Manning class */
+
+/* Length and forcing of a scenario's next iteration, written by the
+ * finalize kernel, read by every tile of the scenario. */
+struct Slot32 {
+    float dt2, dt2dx, dt2dy;
+    float rr1, rr2;     /* rain rate, m/s */
+    float ev1, ev2;     /* evaporation rate, m/s */
+    int active;
+    int cur;            /* which of the two state buffers is current */
+    int pad[7];
+};
+
+struct Clock32 {
+    Slot32 slot;
+    double t, t_end, dt2;     /* dt2: length of the iteration in flight */
+    double s_max;
+    long long iters;
+    double rain_in, source_in, evap_out, outflow, clamp_gain, q_out;
+    double volume0;
+    int status;               /* bit 0 non-finite, bit 1 TMA wait timeout */
+    int done;                 /* set when t reached t_end */
+    long long outlet_n;
+};
+
+/* per work item reduction results */
+struct Part32 {
+    double rain;   /* sum of weight * runoff fraction over active cells (if per cell) */
+    double clamp;  /* depth created by the max(h, 0) clamp */
+    double qout;   /* outlet discharge per unit width summed over the edge faces */
+    double evap;   /* active cells with ho > ev_wl_min (count) */
+    float sx, sy;  /* CFL face-speed maxima of the entering state (x and y faces) */
+    int pad[6];
+};
+
+struct Scn32 {
+    CUtensorMap tm_h[2], tm_qx[2], tm_qy[2], tm_z, tm_info;
+    float* h[2];
+    float* qx[2];
+    float* qy[2];
+    float* kc;             /* Kahan compensation of the depth */
+    const float* datum;    /* per tile, tiles_y * tiles_x */
+    const uint8_t* info;   /* per cell (padded), the TMA-mapped array */
+    const float* rainw;    /* per cell (padded) or NULL */
+    const double* rain;    /* nrain + 2, mm per dtrain */
+    const double* evap;    /* nevap + 2 or NULL */
+    double* outlet;        /* outlet ring (t, Q) or NULL */
+    Clock32* clk;
+    int R, C, P, tiles_x, tiles_y;
+    int first_work, nwork;
+    int outflow_south, ledger_cells, series_mode, dt_mode;
+    int nrain, nevap, outlet_cap;
+    float dx, dy, rdx, rdy, th, g;
+    float pct_lake, pct_land, ev_wl_min;
+    double rain_static;    /* sum over active cells of weight * runoff fraction */
+    double dxd, dyd, dtrain, dt_fixed, cfl, dt_max, area;
+    float ntab[T32_MAXCLASS];
+};
+
+void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, int nwork, Part32* d_part,
+                           cudaStream_t s);
+void fp32_launch_prime(const Scn32* d_scn, int nscn, cudaStream_t s);
+void fp32_launch_volume(const Scn32* d_scn, int iscn, const Scn32& host_scn, double* d_out, cudaStream_t s);
+size_t fp32_smem_bytes();
+int fp32_configure_kernels();
+
+} // namespace sw2d
+#endif

@@ -259,22 +259,71 @@ __device__ __forceinline__ double flux_y(const StepParams& p, const double* __re
     return ((1.00 - dt2 * ram * 0.50) * vn0 + (-v11 - v12 - v13)) / (1.00 + dt2 * ram * 0.50);
 }
 
+__device__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* sm);
+__device__ float block_max_f32_all(float v, float* sm);
+
+/* CFL speed contribution of one face of the entering state: (|velocity| +
+ * sqrt(g * mean depth)) / spacing for faces between two active cells whose
+ * mean depth is >= th (the oracle's cfl_speed, same operations). */
+__device__ __forceinline__ double face_speed(double vel, double hm, double g, double rd) {
+    return (fabs(vel) + sqrt(g * hm)) * rd;
+}
+
+/* exact block maximum of face speeds: binary32 estimate for every face,
+ * binary64 only for the faces within 1e-5 of the block's binary32 maximum */
+__device__ __forceinline__ unsigned long long block_face_speed_max(bool ok, double vel, double hm, double g,
+                                                                   double rd, float* smf,
+                                                                   unsigned long long* smu) {
+    const float s32 = ok ? (fabsf((float)vel) + sqrtf((float)g * (float)hm)) * (float)rd : 0.0f;
+    const float m32 = block_max_f32_all(s32, smf);
+    unsigned long long bits = 0ull;
+    if (ok && s32 >= m32 * 0.99999f) bits = (unsigned long long)__double_as_longlong(face_speed(vel, hm, g, rd));
+    return block_max_u64(bits, smu);
+}
+
 __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_flux(StepParams p, int cur) {
+    __shared__ float smf[SW2D_BX * SW2D_BY / 32];
+    __shared__ unsigned long long smu[SW2D_BX * SW2D_BY / 32];
     const int c = blockIdx.x * SW2D_BX + threadIdx.x;
     const int r = blockIdx.y * SW2D_BY + threadIdx.y;
-    if (r > p.R || c > p.C) return;
-    const size_t i = (size_t)(r + H) * p.P + (c + H);
     const int nxt = cur ^ 1;
     const Slot& s = p.clk->slot[cur];
-    if (!s.active) {
-        if (c < p.C) p.qx[nxt][i] = p.qx[cur][i];
-        if (r < p.R) p.qy[nxt][i] = p.qy[cur][i];
-        return;
+    bool okx = false, oky = false;
+    double hmx = 0, hmy = 0, vx = 0, vy = 0;
+    if (r <= p.R && c <= p.C) {
+        const size_t i = (size_t)(r + H) * p.P + (c + H);
+        if (!s.active) {
+            if (c < p.C) p.qx[nxt][i] = p.qx[cur][i];
+            if (r < p.R) p.qy[nxt][i] = p.qy[cur][i];
+        } else {
+            const double dt2 = s.dt2, dt2dx = s.dt2dx, dt2dy = s.dt2dy;
+            const double* __restrict__ h = p.h[cur];
+            if (c < p.C) p.qx[nxt][i] = flux_x(p, h, p.qx[cur], r, c, i, dt2, dt2dx, dt2dy);
+            if (r < p.R) p.qy[nxt][i] = flux_y(p, h, p.qy[cur], r, c, i, dt2, dt2dx, dt2dy);
+            if (p.dt_mode == 1) {
+                const uint8_t fc = p.flags[i];
+                if (c < p.C && r > 0 && r < p.R && (fc & p.flags[i - p.P] & SW2D_F_ACTIVE)) {
+                    hmx = 0.50 * (h[i] + h[i - p.P]);
+                    okx = hmx >= p.th;
+                    vx = p.uu1[i];
+                }
+                if (r < p.R && c > 0 && c < p.C && (fc & p.flags[i - 1] & SW2D_F_ACTIVE)) {
+                    hmy = 0.50 * (h[i] + h[i - 1]);
+                    oky = hmy >= p.th;
+                    vy = p.vv1[i];
+                }
+            }
+        }
     }
-    const double dt2 = s.dt2, dt2dx = s.dt2dx, dt2dy = s.dt2dy;
-    const double* __restrict__ h = p.h[cur];
-    if (c < p.C) p.qx[nxt][i] = flux_x(p, h, p.qx[cur], r, c, i, dt2, dt2dx, dt2dy);
-    if (r < p.R) p.qy[nxt][i] = flux_y(p, h, p.qy[cur], r, c, i, dt2, dt2dx, dt2dy);
+    if (p.dt_mode == 1) {
+        const unsigned long long sx = block_face_speed_max(okx, vx, hmx, p.g, p.rdx, smf, smu);
+        const unsigned long long sy = block_face_speed_max(oky, vy, hmy, p.g, p.rdy, smf, smu);
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            const int b = blockIdx.y * gridDim.x + blockIdx.x;
+            p.partials_f[2 * b] = __longlong_as_double((long long)sx);
+            p.partials_f[2 * b + 1] = __longlong_as_double((long long)sy);
+        }
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -347,7 +396,7 @@ __device__ __forceinline__ double block_sum(double v, double* sm) {
     return t; /* valid in thread 0 */
 }
 
-__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* sm) {
+__device__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* sm) {
     const int lane = tid_linear() & 31, warp = tid_linear() >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -369,7 +418,7 @@ __device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v
     return t; /* valid in thread 0 */
 }
 
-__device__ __forceinline__ float block_max_f32_all(float v, float* sm) {
+__device__ float block_max_f32_all(float v, float* sm) {
     const int lane = tid_linear() & 31, warp = tid_linear() >> 5;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -380,38 +429,6 @@ __device__ __forceinline__ float block_max_f32_all(float v, float* sm) {
 #pragma unroll
     for (int k = 1; k < NWARP; k++) t = fmaxf(t, sm[k]);
     return t; /* valid in every thread */
-}
-
-/* CFL speed of a wet cell (the oracle's cfl_speed, same operations) */
-__device__ __forceinline__ double cell_speed(const StepParams& p, double fN, double fS, double fW, double fE,
-                                             double hh) {
-    const double qxc = 0.5 * (fN + fS);
-    const double qyc = 0.5 * (fW + fE);
-    return (fabs(qxc) * p.rdx + fabs(qyc) * p.rdy) / hh + sqrt(p.g * hh) * p.rsum;
-}
-
-/* binary32 estimate of cell_speed (relative error < 1e-6), used to select
- * the few cells per block whose exact speed can be the block maximum */
-__device__ __forceinline__ float cell_speed_f32(const StepParams& p, double fN, double fS, double fW, double fE,
-                                                double hh) {
-    const float h = (float)hh;
-    const float qxc = 0.5f * ((float)fN + (float)fS);
-    const float qyc = 0.5f * ((float)fW + (float)fE);
-    return (fabsf(qxc) * (float)p.rdx + fabsf(qyc) * (float)p.rdy) / h + sqrtf((float)p.g * h) * (float)p.rsum;
-}
-
-/* Exact block maximum of the speed: binary32 prefilter, binary64 for the
- * candidates within 1e-5 of the block's binary32 maximum, maximum over the
- * IEEE bit patterns (the speeds are non-negative). */
-__device__ __forceinline__ unsigned long long block_speed_max(const StepParams& p, bool wet, double fN, double fS,
-                                                              double fW, double fE, double hh) {
-    __shared__ float smf[NWARP];
-    __shared__ unsigned long long smu[NWARP];
-    const float s32 = wet ? cell_speed_f32(p, fN, fS, fW, fE, hh) : 0.0f;
-    const float m32 = block_max_f32_all(s32, smf);
-    unsigned long long bits = 0ull;
-    if (wet && s32 >= m32 * 0.99999f) bits = (unsigned long long)__double_as_longlong(cell_speed(p, fN, fS, fW, fE, hh));
-    return block_max_u64(bits, smu);
 }
 
 #define NPART 4 /* rain, evap, qout, s_max bits */
@@ -438,21 +455,32 @@ __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
         vr += pb[0];
         ve += pb[1];
         vq += pb[2];
-        unsigned long long u = (unsigned long long)__double_as_longlong(pb[3]);
-        vs = u > vs ? u : vs;
     }
     if (p.ledger_cells) {
         vr = block_sum(vr, smd);
         ve = block_sum(ve, smd);
     }
     if (p.outflow_south) vq = block_sum(vq, smd);
-    vs = block_max_u64(vs, smu);
+    /* CFL speed of the state this iteration started from, from k64_flux */
+    unsigned long long ux = 0ull, uy = 0ull;
+    if (p.dt_mode == 1) {
+        for (int b = tid; b < p.nblocks_faces; b += SW2D_BX * SW2D_BY) {
+            const volatile double* pb = p.partials_f + (size_t)b * 2;
+            unsigned long long a = (unsigned long long)__double_as_longlong(pb[0]);
+            unsigned long long c = (unsigned long long)__double_as_longlong(pb[1]);
+            ux = a > ux ? a : ux;
+            uy = c > uy ? c : uy;
+        }
+        ux = block_max_u64(ux, smu);
+        uy = block_max_u64(uy, smu);
+    }
+    (void)vs;
     if (tid == 0) {
         DevClock* clk = p.clk;
         const Slot& s = clk->slot[cur];
         if (s.active) {
             const double dt2 = s.dt2;
-            const double smax = __longlong_as_double((long long)vs);
+            const double smax = __longlong_as_double((long long)ux) + __longlong_as_double((long long)uy);
             double src = 0.0;
             for (int k = 0; k < p.nsrc; k++) src += s.ql2[k];
             const double rain = p.ledger_cells ? vr : s.rr2 * p.rain_static;
@@ -532,7 +560,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_depth(StepParams p, int
         pe = block_sum(ve, smd);
     }
     if (p.outflow_south && (blockIdx.y + 1) * SW2D_BY >= p.R) pq = block_sum(vq, smd);
-    const unsigned long long sb = (p.dt_mode == 1) ? block_speed_max(p, wet, fN, fS, fW, fE, hn) : 0ull;
+    (void)wet;
     const int tid = tid_linear();
     const int b = blockIdx.y * gridDim.x + blockIdx.x;
     if (tid == 0) {
@@ -540,41 +568,51 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_depth(StepParams p, int
         pb[0] = pr;
         pb[1] = pe;
         pb[2] = pq;
-        pb[3] = __longlong_as_double((long long)sb);
     }
     finish_iteration(p, cur, gridDim.x * gridDim.y);
 }
 
 /* Volume (sum of h over active cells) and, with full, the CFL speed of the
- * current state; the last block stores them and prepares the next slot. */
+ * current state (face rule of k64_flux); the last block stores them and
+ * prepares the next slot. */
 __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int cur, int full) {
     __shared__ double smd[NWARP];
+    __shared__ float smf[NWARP];
     __shared__ unsigned long long smu[NWARP];
     __shared__ bool last;
     const int c = blockIdx.x * SW2D_BX + threadIdx.x;
     const int r = blockIdx.y * SW2D_BY + threadIdx.y;
     double vol = 0.0;
-    unsigned long long sb = 0ull;
+    bool okx = false, oky = false;
+    double hmx = 0, hmy = 0, vx = 0, vy = 0;
     if (full && r < p.R && c < p.C) {
         const int P = p.P;
         const size_t i = (size_t)(r + H) * P + (c + H);
-        const double hh = p.h[cur][i];
-        if ((p.flags[i] & SW2D_F_ACTIVE)) {
-            vol = hh;
-            if (hh >= p.th) {
-                const double* fx = p.qx[cur];
-                const double* fy = p.qy[cur];
-                sb = (unsigned long long)__double_as_longlong(cell_speed(p, fx[i], fx[i + P], fy[i], fy[i + 1], hh));
+        const double* h = p.h[cur];
+        const uint8_t fc = p.flags[i];
+        if (fc & SW2D_F_ACTIVE) {
+            vol = h[i];
+            if (r > 0 && (p.flags[i - P] & SW2D_F_ACTIVE)) {
+                hmx = 0.50 * (h[i] + h[i - P]);
+                okx = hmx >= p.th;
+                vx = p.uu1[i];
+            }
+            if (c > 0 && (p.flags[i - 1] & SW2D_F_ACTIVE)) {
+                hmy = 0.50 * (h[i] + h[i - 1]);
+                oky = hmy >= p.th;
+                vy = p.vv1[i];
             }
         }
     }
     vol = block_sum(vol, smd);
-    sb = block_max_u64(sb, smu);
+    const unsigned long long sx = block_face_speed_max(okx, vx, hmx, p.g, p.rdx, smf, smu);
+    const unsigned long long sy = block_face_speed_max(oky, vy, hmy, p.g, p.rdy, smf, smu);
     const int tid = tid_linear();
     const int b = blockIdx.y * gridDim.x + blockIdx.x;
     if (tid == 0) {
         p.partials[(size_t)b * NPART + 0] = vol;
-        p.partials[(size_t)b * NPART + 3] = __longlong_as_double((long long)sb);
+        p.partials[(size_t)b * NPART + 1] = __longlong_as_double((long long)sx);
+        p.partials[(size_t)b * NPART + 2] = __longlong_as_double((long long)sy);
     }
     __threadfence();
     if (tid == 0) last = (atomicAdd(&p.clk->counter, 1u) == gridDim.x * gridDim.y - 1);
@@ -583,19 +621,22 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int
     __threadfence();
     const int nb = gridDim.x * gridDim.y;
     double v = 0.0;
-    unsigned long long u = 0ull;
+    unsigned long long ux = 0ull, uy = 0ull;
     for (int bb = tid; bb < nb; bb += SW2D_BX * SW2D_BY) {
         const volatile double* pb = p.partials + (size_t)bb * NPART;
         v += pb[0];
-        unsigned long long w = (unsigned long long)__double_as_longlong(pb[3]);
-        u = w > u ? w : u;
+        unsigned long long a = (unsigned long long)__double_as_longlong(pb[1]);
+        unsigned long long w = (unsigned long long)__double_as_longlong(pb[2]);
+        ux = a > ux ? a : ux;
+        uy = w > uy ? w : uy;
     }
     v = block_sum(v, smd);
-    u = block_max_u64(u, smu);
+    ux = block_max_u64(ux, smu);
+    uy = block_max_u64(uy, smu);
     if (tid == 0) {
         DevClock* clk = p.clk;
         if (full) {
-            clk->s_max = __longlong_as_double((long long)u);
+            clk->s_max = __longlong_as_double((long long)ux) + __longlong_as_double((long long)uy);
             clk->led[LED_SMAX] = clk->s_max;
             clk->led[LED_VOLUME] = v * p.area;
             if (full == 2) clk->led[LED_VOLUME0] = clk->led[LED_VOLUME];

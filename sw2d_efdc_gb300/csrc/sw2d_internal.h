@@ -92,7 +92,9 @@ struct StepParams {
     double* uu1;
     double* vv1;
     uint8_t* drys;
-    double* partials;      /* nblocks_cells * 8 */
+    double* partials;      /* nblocks_cells * 4: rain, evaporation, outlet sums */
+    double* partials_f;    /* nblocks_faces * 2: CFL face-speed maxima (bit patterns) */
+    int nblocks_faces;
     double* outlet;        /* outlet_cap * 2 or NULL */
     DevClock* clk;
 };

@@ -1,0 +1,91 @@
+"""FP32 precision form (fused TMA tile kernel) against the FP64 path and the
+oracle, through the C ABI.
+
+Tolerances: the FP32 form is not bit-compatible; it must stay within
+1 mm of the FP64 depth on these short runs, conserve volume to 1e-6 of the
+inflow, and choose CFL iteration lengths within 1e-4 of the FP64 ones.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from sw2d_efdc_gb300 import api
+from tests.helpers import bumpy_case, model_from_case
+
+pytestmark = pytest.mark.gpu
+
+DEPTH_TOL = 1e-3  # m
+
+
+def _pair(case, iters=None):
+    m64 = model_from_case(case, precision=api.FP64)
+    m32 = model_from_case(case, precision=api.FP32)
+    if iters is None:
+        n64 = m64.advance(case.t_end)
+        n32 = m32.advance(case.t_end)
+    else:
+        m64.step(iters + (iters & 1), case.t_end)
+        m32.step(iters + (iters & 1), case.t_end)
+        n64 = n32 = iters
+    return m64, m32, n64, n32
+
+
+def test_fp32_tracks_fp64_fixed_dt_multi_tile():
+    # 100 x 150: partial tiles in both directions, NODATA holes across tile edges
+    case = bumpy_case(R=100, C=150, seed=21, t_end=120.0, dt=0.05)
+    case.dem[30:36, 60:70] = -9999.0
+    case.h0[case.dem == -9999.0] = 0
+    m64, m32, n64, n32 = _pair(case)
+    assert n64 == n32
+    h64, h32 = m64.depth(), m32.depth()
+    assert np.abs(h64 - h32).max() < DEPTH_TOL
+    wet64, wet32 = h64 > 1e-3, h32 > 1e-3
+    assert (wet64 != wet32).mean() < 1e-3
+    _, qx64, qy64 = m64.state()
+    _, qx32, qy32 = m32.state()
+    assert np.abs(qx64 - qx32).max() < 5e-3
+    led = m32.ledger()
+    assert abs(led["balance_error"]) < 1e-6, led
+
+
+def test_fp32_high_bed_uses_tile_datum():
+    # a catchment at 800-900 m: absolute binary32 elevations would carry
+    # 6e-5 m rounding; the per-tile datum keeps the depth error small
+    case = bumpy_case(R=70, C=90, seed=22, t_end=60.0, dt=0.05, holes=False)
+    case.dem = case.dem + 850.0
+    m64, m32, _, _ = _pair(case)
+    assert np.abs(m64.depth() - m32.depth()).max() < DEPTH_TOL
+
+
+def test_fp32_cfl_outflow_rain_field_classes():
+    rng = np.random.default_rng(5)
+    case = bumpy_case(R=96, C=130, seed=23, dt_mode=O.DT_CFL, cfl=0.7, dt_max=1.5, outflow_south=True,
+                      rain_mode=O.RAIN_STEP, rain=np.array([8.0, 8.0, 0.0, 4.0]), dtrain=30.0, t_end=150.0,
+                      holes=False)
+    case.manning_field = rng.choice([0.02, 0.05, 0.10], size=case.dem.shape)
+    case.rain_weight = (0.5 + rng.random(case.dem.shape)).astype(np.float32)
+    m64, m32, n64, n32 = _pair(case)
+    assert abs(n64 - n32) <= max(2, 0.01 * n64)
+    assert m32.time()[0] == pytest.approx(150.0, abs=1e-9)
+    assert np.abs(m64.depth() - m32.depth()).max() < DEPTH_TOL
+    l64, l32 = m64.ledger(), m32.ledger()
+    assert l32["outflow"] == pytest.approx(l64["outflow"], rel=1e-3, abs=1e-3)
+    assert abs(l32["balance_error"]) < 1e-6
+    assert l32["s_max"] == pytest.approx(l64["s_max"], rel=1e-4)
+
+
+def test_fp32_oracle_volume_and_outlet():
+    case = bumpy_case(R=64, C=64, seed=24, dt_mode=O.DT_CFL, cfl=0.7, dt_max=2.0, outflow_south=True,
+                      rain_mode=O.RAIN_STEP, rain=np.array([20.0, 20.0, 0.0]), dtrain=60.0, t_end=200.0,
+                      holes=False)
+    m32 = model_from_case(case, precision=api.FP32)
+    m32.set_outlet_record(8192)
+    n = m32.advance(case.t_end)
+    o = O.Oracle(case, math=O.MATH_DEVICE)
+    o.run()
+    assert abs(n - o.iters) <= 2
+    t32, q32 = m32.outlet()
+    to, qo = o.outlet()
+    assert len(t32) == n
+    assert np.abs(np.interp(to, t32, q32) - qo).max() < 1e-3 * max(qo.max(), 1e-9) + 1e-6
+    assert m32.ledger()["volume"] == pytest.approx(o.ledger()["volume"], rel=1e-4)
