@@ -1,0 +1,81 @@
+/* sw2d_batch.h -- batched and served FP32 SW2D through one C ABI.
+ *
+ * The reference advances one raster per process and has no batching or
+ * request interface: main() loops over the cases listed in db/dir.txt one
+ * after the other (SW2D-EFDC.cu:3733-3738) and calls the step kernels of
+ * SW2D-EFDC.cu:97-725 for each.  This interface runs many scenarios of
+ * uneven raster sizes together on one GPU: every iteration is one launch of
+ * the fused FP32 tile kernel over all running scenarios, each with its own
+ * CFL iteration length and forcing.
+ *
+ * Requests are admitted as HBM (the budget given at creation) and running
+ * slots free up; their state stays on the device until they reach their end
+ * time, when the final fields move to host memory and the device memory is
+ * released.  One batch is driven by one host thread at a time.
+ */
+#ifndef SW2D_BATCH_H
+#define SW2D_BATCH_H
+
+#include <stdint.h>
+
+#include "sw2d.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { SW2D_REQ_QUEUED = 0, SW2D_REQ_RUNNING = 1, SW2D_REQ_DONE = 2, SW2D_REQ_FAILED = 3 };
+
+/* One scenario: the fields of sw2d_config plus its inputs.  Host arrays are
+ * copied by sw2d_batch_submit. */
+typedef struct sw2d_scenario {
+    int rows, cols;
+    int dt_mode;              /* SW2D_DT_* */
+    int series_mode;          /* SW2D_SERIES_* */
+    int outflow;              /* SW2D_OUTFLOW_* */
+    int ntable;               /* Manning classes (<= 64), 0 = uniform */
+    int nrain;
+    int outlet_capacity;      /* outlet hydrograph ring, 0 = none */
+    double dx, dy, nodata, th, g, manning;
+    double dt, cfl, dt_max, t0, t_end;
+    double frac_int, frac_inf, frac_lwl, ev_wl_min;
+    double dtrain;
+    const double* dem;        /* rows*cols, row 0 = north */
+    const double* depth;      /* rows*cols or NULL (dry) */
+    const uint8_t* manning_class;
+    const double* manning_table;
+    const double* rain_mm;    /* nrain values, mm per dtrain */
+    const float* rain_weight; /* rows*cols or NULL */
+} sw2d_scenario;
+
+typedef struct sw2d_batch_stats {
+    int running, queued;
+    int work_items;           /* tiles per iteration */
+    int reserved;
+    double bytes_in_use;
+    double device_ms;         /* device time of all iterations so far */
+    double cell_updates;      /* sum over scenarios of cells x iterations advanced */
+    double launches;          /* kernel launches issued */
+} sw2d_batch_stats;
+
+typedef struct sw2d_batch sw2d_batch;
+
+/* max_running = 0: no limit besides the HBM budget (0 = no budget). */
+int sw2d_batch_create(int device, double hbm_budget_bytes, int max_running, sw2d_batch** out);
+int sw2d_batch_destroy(sw2d_batch* b);
+int sw2d_batch_submit(sw2d_batch* b, const sw2d_scenario* s, int64_t* id_out);
+/* Admit what fits, advance every running scenario by `iterations`
+ * iterations, retire the finished ones. */
+int sw2d_batch_step(sw2d_batch* b, int iterations, int* n_running_out, int* n_queued_out);
+int sw2d_batch_poll(sw2d_batch* b, int64_t id, int* status, sw2d_ledger* ledger);
+/* Final fields of a finished request: depth rows*cols, qx (rows+1)*cols,
+ * qy rows*(cols+1), reference orientation; any pointer may be NULL. */
+int sw2d_batch_result(sw2d_batch* b, int64_t id, double* depth, double* qx, double* qy);
+int sw2d_batch_release(sw2d_batch* b, int64_t id);
+int sw2d_batch_get_stats(sw2d_batch* b, sw2d_batch_stats* out);
+const char* sw2d_batch_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SW2D_BATCH_H */

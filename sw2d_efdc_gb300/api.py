@@ -53,6 +53,29 @@ class Ledger(C.Structure):
         "clamp_gain", "q_out", "s_max", "dt_last", "balance_error")]
 
 
+class Scenario(C.Structure):
+    _fields_ = [
+        ("rows", C.c_int), ("cols", C.c_int), ("dt_mode", C.c_int), ("series_mode", C.c_int),
+        ("outflow", C.c_int), ("ntable", C.c_int), ("nrain", C.c_int), ("outlet_capacity", C.c_int),
+        ("dx", C.c_double), ("dy", C.c_double), ("nodata", C.c_double), ("th", C.c_double),
+        ("g", C.c_double), ("manning", C.c_double), ("dt", C.c_double), ("cfl", C.c_double),
+        ("dt_max", C.c_double), ("t0", C.c_double), ("t_end", C.c_double), ("frac_int", C.c_double),
+        ("frac_inf", C.c_double), ("frac_lwl", C.c_double), ("ev_wl_min", C.c_double),
+        ("dtrain", C.c_double),
+        ("dem", C.POINTER(C.c_double)), ("depth", C.POINTER(C.c_double)),
+        ("manning_class", C.POINTER(C.c_uint8)), ("manning_table", C.POINTER(C.c_double)),
+        ("rain_mm", C.POINTER(C.c_double)), ("rain_weight", C.POINTER(C.c_float)),
+    ]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("running", C.c_int), ("queued", C.c_int), ("work_items", C.c_int), ("reserved", C.c_int),
+                ("bytes_in_use", C.c_double), ("device_ms", C.c_double), ("cell_updates", C.c_double),
+                ("launches", C.c_double)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
 _dp = C.POINTER(C.c_double)
 _fp = C.POINTER(C.c_float)
 _ip = C.POINTER(C.c_int)
@@ -91,6 +114,16 @@ SIGNATURES = {
     "sw2d_restore": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "sw2d_get_timing": (C.c_int, [C.c_void_p, _dp, _dp, _ip]),
     "sw2d_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    # include/sw2d_batch.h
+    "sw2d_batch_create": (C.c_int, [C.c_int, C.c_double, C.c_int, C.POINTER(C.c_void_p)]),
+    "sw2d_batch_destroy": (C.c_int, [C.c_void_p]),
+    "sw2d_batch_submit": (C.c_int, [C.c_void_p, C.POINTER(Scenario), _i64p]),
+    "sw2d_batch_step": (C.c_int, [C.c_void_p, C.c_int, _ip, _ip]),
+    "sw2d_batch_poll": (C.c_int, [C.c_void_p, C.c_int64, _ip, C.POINTER(Ledger)]),
+    "sw2d_batch_result": (C.c_int, [C.c_void_p, C.c_int64, _dp, _dp, _dp]),
+    "sw2d_batch_release": (C.c_int, [C.c_void_p, C.c_int64]),
+    "sw2d_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
+    "sw2d_batch_last_error": (C.c_char_p, []),
 }
 
 _lib = None
@@ -299,3 +332,98 @@ class Model:
         nk = C.c_int()
         _check(load().sw2d_get_timing(self._h, C.byref(ms), _ptr(per, _dp), C.byref(nk)), "sw2d_get_timing")
         return ms.value, per[: nk.value]
+
+
+def _bcheck(code: int, where: str):
+    if code != 0:
+        raise Sw2dError(code, where, load().sw2d_batch_last_error().decode(errors="replace"))
+
+
+class Batch:
+    """Many FP32 scenarios advanced together, with HBM-budget admission."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0.0, max_running=0):
+        h = C.c_void_p()
+        _bcheck(load().sw2d_batch_create(int(device), float(hbm_budget_bytes), int(max_running), C.byref(h)),
+                "sw2d_batch_create")
+        self._h = h
+        self._shapes = {}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            load().sw2d_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, dem, depth=None, manning=0.03, manning_classes=None, manning_table=None, rain_mm=(0.0,),
+               dtrain=3600.0, rain_weight=None, dx=1.0, dy=None, t_end=3600.0, dt_mode=DT_CFL,
+               series_mode=SERIES_STEP, outflow=OUTFLOW_NONE, cfl=0.7, dt_max=2.0, dt=0.04, t0=0.0,
+               nodata=-9999.0, th=1e-4, g=9.80, outlet_capacity=0, frac_int=0.0, frac_inf=0.0,
+               frac_lwl=0.0, ev_wl_min=0.05) -> int:
+        dem = np.ascontiguousarray(dem, np.float64)
+        R, Cc = dem.shape
+        keep = [dem]
+        s = Scenario()
+        s.rows, s.cols = R, Cc
+        s.dt_mode, s.series_mode, s.outflow = dt_mode, series_mode, outflow
+        s.dx = dx
+        s.dy = dx if dy is None else dy
+        s.nodata, s.th, s.g, s.manning = nodata, th, g, manning
+        s.dt, s.cfl, s.dt_max, s.t0, s.t_end = dt, cfl, dt_max, t0, t_end
+        s.frac_int, s.frac_inf, s.frac_lwl, s.ev_wl_min = frac_int, frac_inf, frac_lwl, ev_wl_min
+        s.dtrain = dtrain
+        s.outlet_capacity = outlet_capacity
+        s.dem = _ptr(dem, _dp)
+        if depth is not None:
+            depth = np.ascontiguousarray(depth, np.float64)
+            keep.append(depth)
+            s.depth = _ptr(depth, _dp)
+        if manning_classes is not None:
+            cl = np.ascontiguousarray(manning_classes, np.uint8)
+            tb = np.ascontiguousarray(manning_table, np.float64)
+            keep += [cl, tb]
+            s.manning_class, s.manning_table, s.ntable = _ptr(cl, _u8p), _ptr(tb, _dp), len(tb)
+        rain = np.ascontiguousarray(rain_mm, np.float64)
+        keep.append(rain)
+        s.rain_mm, s.nrain = _ptr(rain, _dp), len(rain)
+        if rain_weight is not None:
+            w = np.ascontiguousarray(rain_weight, np.float32)
+            keep.append(w)
+            s.rain_weight = _ptr(w, _fp)
+        rid = C.c_int64(0)
+        _bcheck(load().sw2d_batch_submit(self._h, C.byref(s), C.byref(rid)), "sw2d_batch_submit")
+        self._shapes[rid.value] = (R, Cc)
+        return rid.value
+
+    def step(self, iterations):
+        nr, nq = C.c_int(0), C.c_int(0)
+        _bcheck(load().sw2d_batch_step(self._h, int(iterations), C.byref(nr), C.byref(nq)), "sw2d_batch_step")
+        return nr.value, nq.value
+
+    def poll(self, rid):
+        st = C.c_int(0)
+        L = Ledger()
+        _bcheck(load().sw2d_batch_poll(self._h, int(rid), C.byref(st), C.byref(L)), "sw2d_batch_poll")
+        return st.value, {n: getattr(L, n) for n, _ in Ledger._fields_}
+
+    def result(self, rid):
+        R, Cc = self._shapes[rid]
+        h = np.empty((R, Cc))
+        qx = np.empty((R + 1, Cc))
+        qy = np.empty((R, Cc + 1))
+        _bcheck(load().sw2d_batch_result(self._h, int(rid), _ptr(h, _dp), _ptr(qx, _dp), _ptr(qy, _dp)),
+                "sw2d_batch_result")
+        return h, qx, qy
+
+    def release(self, rid):
+        _bcheck(load().sw2d_batch_release(self._h, int(rid)), "sw2d_batch_release")
+
+    def stats(self) -> dict:
+        st = BatchStats()
+        _bcheck(load().sw2d_batch_get_stats(self._h, C.byref(st)), "sw2d_batch_get_stats")
+        return {n: getattr(st, n) for n, _ in BatchStats._fields_}

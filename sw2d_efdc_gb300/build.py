@@ -29,6 +29,7 @@ UNITS = {
     "sw2d_fp64.cu": ["--fmad=false", "-Xptxas", "-v"],
     "sw2d_fp32.cu": ["-Xptxas", "-v"],
     "sw2d_engine.cu": [],
+    "sw2d_batch.cu": [],
     "sw2d_api.cu": [],
 }
 HEADERS = ["sw2d_internal.h", "sw2d_math.h", "sw2d_fp32.h", "sw2d_engine.h"]
@@ -49,7 +50,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 def _compile(unit: str) -> tuple[str, str]:
     src = os.path.join(CSRC, unit)
     obj = os.path.join(OBJ_DIR, unit.replace(".cu", ".o"))
-    deps = [src, os.path.join(ROOT, "include", "sw2d.h")] + [os.path.join(CSRC, h) for h in HEADERS]
+    deps = [src, os.path.join(ROOT, "include", "sw2d.h"), os.path.join(ROOT, "include", "sw2d_batch.h")] + \
+        [os.path.join(CSRC, h) for h in HEADERS]
     if not _stale(obj, deps + [__file__]):
         return obj, ""
     cmd = [nvcc()] + ARCH + COMMON + UNITS[unit] + ["-c", src, "-o", obj + ".tmp"]

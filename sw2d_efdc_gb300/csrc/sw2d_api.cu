@@ -367,13 +367,14 @@ int run_until_fp32(sw2d_handle* h, double t_end, long long max_iters, int64_t* d
             ms += h->eng->last_ms();
             if ((rc = h->eng->get_clock(h->eng_idx, &c, &err))) return fail(rc, err);
             if (c.done || !c.slot.active) break;
-            if (c.status & 3) break;
+            if (c.status & 7) break;
         }
     }
     if ((rc = h->eng->get_clock(h->eng_idx, &c, &err))) return fail(rc, err);
     const long long done = c.iters - c0.iters;
     h->last_ms_per_iter = done > 0 ? ms / (double)done : 0.0;
     if (done_out) *done_out = done;
+    if (c.status & 4) return fail(SW2D_ERR_CUDA, "FP32 tile staging buffer misaligned (tiles skipped)");
     if (c.status & 2) return fail(SW2D_ERR_TIMEOUT, "a tile's staged load did not arrive in time");
     if (c.status & 1) return fail(SW2D_ERR_NUMERIC, "non-finite state");
     return SW2D_OK;

@@ -25,6 +25,7 @@
 #include "sw2d_fp32.h"
 
 #include <math.h>
+#include <stddef.h>
 
 namespace sw2d {
 
@@ -47,14 +48,16 @@ namespace sw2d {
 #define FY_W 67 /* y faces rows [3, 37), cols [3, 70) */
 #define FY_H 34
 
+/* TMA tensor copies need 128-byte aligned shared destinations: the five
+ * staged arrays come first, each a multiple of 128 bytes long. */
 struct Smem32 {
-    float h[LH * LW];
-    float z[LH * LW];
-    float qx[LH * LW];
-    float qy[LH * LW];
-    float u[U_H * U_W];
+    alignas(128) float h[LH * LW];
+    alignas(128) float z[LH * LW];
+    alignas(128) float qx[LH * LW];
+    alignas(128) float qy[LH * LW];
+    alignas(128) uint8_t info[LH * LWB];
+    alignas(128) float u[U_H * U_W];
     float v[V_H * V_W];
-    uint8_t info[LH * LWB];
     uint8_t dry[D_H * D_W];
     float ntab[T32_MAXCLASS];
     float dd[9];
@@ -62,6 +65,11 @@ struct Smem32 {
     float redf[8][2];
     unsigned long long bar;
 };
+static_assert(offsetof(Smem32, h) % 128 == 0 && offsetof(Smem32, z) % 128 == 0, "TMA alignment");
+static_assert(offsetof(Smem32, qx) % 128 == 0 && offsetof(Smem32, qy) % 128 == 0, "TMA alignment");
+static_assert(offsetof(Smem32, info) % 128 == 0, "TMA alignment");
+static_assert(offsetof(Smem32, bar) % 8 == 0, "mbarrier alignment");
+static_assert((LH * LW * 4) % 128 == 0 && (LH * LWB) % 128 == 0, "staged arrays are whole 128-byte lines");
 
 size_t fp32_smem_bytes() { return sizeof(Smem32) + 128; }
 
@@ -262,6 +270,12 @@ __global__ void __launch_bounds__(NT, 3) k32_step(const Scn32* __restrict__ scns
     const int tx = w.y, ty = w.z;
     const int c0 = tx * TC, r0 = ty * TR;
 
+    /* self-check of the staging layout: a misaligned TMA destination would
+     * fault, so record it and skip the tile instead */
+    if (((smem_addr(S.h) | smem_addr(S.z) | smem_addr(S.qx) | smem_addr(S.qy) | smem_addr(S.info)) & 127u) != 0u) {
+        if (tid == 0) atomicOr(&clk->status, 4);
+        return;
+    }
     if (tid == 0) {
         mbar_init(&S.bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");

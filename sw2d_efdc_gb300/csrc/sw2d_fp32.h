@@ -50,7 +50,7 @@ struct Clock32 {
     long long iters;
     double rain_in, source_in, evap_out, outflow, clamp_gain, q_out;
     double volume0;
-    int status;               /* bit 0 non-finite, bit 1 TMA wait timeout */
+    int status;               /* bit 0 non-finite, bit 1 TMA wait timeout, bit 2 misaligned staging */
     int done;                 /* set when t reached t_end */
     long long outlet_n;
 };
