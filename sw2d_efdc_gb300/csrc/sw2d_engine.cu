@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 
 namespace sw2d {
 
@@ -27,7 +28,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 bool make_map(CUtensorMap* tm, void* base, CUtensorMapDataType dt, size_t esize, uint64_t width, uint64_t height,
-              uint32_t boxw, uint32_t boxh) {
+              uint32_t boxw, uint32_t boxh, bool nan_fill) {
     auto fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[2] = {width, height};
@@ -35,10 +36,12 @@ bool make_map(CUtensorMap* tm, void* base, CUtensorMapDataType dt, size_t esize,
     cuuint32_t box[2] = {boxw, boxh};
     cuuint32_t es[2] = {1, 1};
     return fn(tm, dt, 2, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+              CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              nan_fill ? CU_TENSOR_MAP_FLOAT_OOB_FILL_NAN_REQUEST_ZERO_FMA : CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
 }
 
-int pitch_of(int cols) { return ((cols + 2 * T32_H + 31) / 32) * 32; }
+int pitch_of(int cols) { return ((cols + 12 + 31) / 32) * 32; }
 
 #define ECK(call)                                                                   \
     do {                                                                            \
@@ -86,11 +89,11 @@ int Engine32::init(std::string* err) {
 }
 
 size_t Engine32::scenario_bytes(int rows, int cols, bool rain_field, int outlet_cap) {
-    const size_t P = pitch_of(cols), NR = rows + 2 * T32_H;
+    const size_t P = pitch_of(cols), NR = rows + 2 * M_H;
     const size_t cells = P * NR;
-    size_t b = cells * (8 * sizeof(float) + 1);
+    size_t b = cells * (8 * sizeof(float) + 1); /* 8 float fields + optional Manning class byte */
     if (rain_field) b += cells * sizeof(float);
-    const size_t tiles = (size_t)((cols + T32_TC - 1) / T32_TC) * ((rows + T32_TR - 1) / T32_TR);
+    const size_t tiles = (size_t)((cols + M_CW - 1) / M_CW) * ((rows + 15) / 16);
     b += tiles * sizeof(float) + (size_t)outlet_cap * 16 + sizeof(Clock32) + 4096;
     return b;
 }
@@ -114,13 +117,14 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     auto sp = std::make_unique<Scenario32>();
     Scenario32& S = *sp;
     S.id = id;
-    const int R = in.rows, C = in.cols, P = pitch_of(C), NR = R + 2 * T32_H;
+    const int R = in.rows, C = in.cols, P = pitch_of(C), NR = R + 2 * M_H;
     S.R = R;
     S.C = C;
     S.P = P;
     S.NR = NR;
     const size_t cells = (size_t)P * NR;
-    const int tx = (C + T32_TC - 1) / T32_TC, ty = (R + T32_TR - 1) / T32_TR;
+    const int seg = seg_rows_ > 0 ? seg_rows_ : 128;
+    const int tx = (C + M_CW - 1) / M_CW, ty = (R + seg - 1) / seg;
     auto alloc = [&](size_t bytes, void** p) -> int {
         cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
         if (e != cudaSuccess) {
@@ -153,10 +157,13 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     float* dz;
     if ((rc = alloc(cells * 4, &p))) return fail_free(rc);
     dz = (float*)p;
-    uint8_t* dinfo;
-    if ((rc = alloc(cells, &p))) return fail_free(rc);
-    dinfo = (uint8_t*)p;
-    d.info = dinfo;
+    d.z = dz;
+    uint8_t* dcls = nullptr;
+    if (in.mclass) {
+        if ((rc = alloc(cells, &p))) return fail_free(rc);
+        dcls = (uint8_t*)p;
+    }
+    d.cls = dcls;
     float* ddatum;
     if ((rc = alloc((size_t)tx * ty * 4, &p))) return fail_free(rc);
     ddatum = (float*)p;
@@ -183,17 +190,19 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     dclk = (Clock32*)p;
     d.clk = dclk;
 
-    /* host staging: per-tile datum (multiple of 1/16 m), bed offsets, info */
+    /* host staging: per-tile datum (a multiple of 1/16 m) over the kernel's
+     * (strip, segment) tiles, bed offsets with NaN for inactive cells */
     std::vector<float> datum((size_t)tx * ty, 0.f);
-    std::vector<float> zoff(cells, 0.f), hbuf(cells, 0.f), rw;
-    std::vector<uint8_t> info(cells, 0);
+    std::vector<float> zoff(cells, std::numeric_limits<float>::quiet_NaN()), hbuf(cells, 0.f), rw;
+    std::vector<uint8_t> cls;
+    if (in.mclass) cls.assign(cells, 0);
     double active_weight = 0.0;
     for (int j = 0; j < ty; j++)
         for (int i = 0; i < tx; i++) {
             double sum = 0;
             long n = 0;
-            for (int r = j * T32_TR; r < std::min(R, (j + 1) * T32_TR); r++)
-                for (int c = i * T32_TC; c < std::min(C, (i + 1) * T32_TC); c++) {
+            for (int r = j * seg; r < std::min(R, (j + 1) * seg); r++)
+                for (int c = i * M_CW; c < std::min(C, (i + 1) * M_CW); c++) {
                     double z = in.dem[(size_t)r * C + c];
                     if (z != in.nodata) {
                         sum += z;
@@ -202,27 +211,29 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
                 }
             datum[(size_t)j * tx + i] = n ? (float)(std::round(sum / n * 16.0) / 16.0) : 0.f;
         }
-    if (in.rain_weight) rw.assign(cells, 0.f);
+    if (in.rain_weight) rw.assign(cells, 1.f);
     for (int r = 0; r < R; r++)
         for (int c = 0; c < C; c++) {
             const size_t k = (size_t)r * C + c;
-            const size_t g = (size_t)(r + T32_H) * P + (c + T32_H);
+            const size_t g = (size_t)(r + M_H) * P + (c + M_H);
             const double z = in.dem[k];
             const bool act = z != in.nodata;
-            const double dat = datum[(size_t)(r / T32_TR) * tx + (c / T32_TC)];
-            zoff[g] = act ? (float)(z - dat) : 0.f;
-            uint8_t cls = in.mclass ? in.mclass[k] : 0;
-            if (in.mclass && cls >= in.ntable) {
-                if (err) *err = "Manning class out of table range";
-                return fail_free(SW2D_ERR_INVALID);
+            const double dat = datum[(size_t)(r / seg) * tx + (c / M_CW)];
+            if (act) zoff[g] = (float)(z - dat);
+            if (in.mclass) {
+                const uint8_t cl = in.mclass[k];
+                if (cl >= in.ntable) {
+                    if (err) *err = "Manning class out of table range";
+                    return fail_free(SW2D_ERR_INVALID);
+                }
+                cls[g] = cl;
             }
-            info[g] = (uint8_t)((act ? SW2D_I_ACTIVE : 0) | (cls << 1));
             hbuf[g] = (act && in.depth) ? (float)in.depth[k] : 0.f;
             if (in.rain_weight) rw[g] = in.rain_weight[k];
             if (act) active_weight += in.rain_weight ? (double)in.rain_weight[k] : 1.0;
         }
     ECK(cudaMemcpyAsync(dz, zoff.data(), cells * 4, cudaMemcpyHostToDevice, stream_));
-    ECK(cudaMemcpyAsync(dinfo, info.data(), cells, cudaMemcpyHostToDevice, stream_));
+    if (dcls) ECK(cudaMemcpyAsync(dcls, cls.data(), cells, cudaMemcpyHostToDevice, stream_));
     ECK(cudaMemcpyAsync(d.h[0], hbuf.data(), cells * 4, cudaMemcpyHostToDevice, stream_));
     ECK(cudaMemcpyAsync(ddatum, datum.data(), datum.size() * 4, cudaMemcpyHostToDevice, stream_));
     if (drw) ECK(cudaMemcpyAsync(drw, rw.data(), cells * 4, cudaMemcpyHostToDevice, stream_));
@@ -230,15 +241,15 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     for (int k = 0; k < in.nrain; k++) rain[k] = in.rain[k];
     ECK(cudaMemcpyAsync(drain, rain.data(), rain.size() * 8, cudaMemcpyHostToDevice, stream_));
 
-    /* tensor maps: fields staged as 72 x 40 tiles, the info byte as 80 x 40 */
+    /* tensor maps: rows of 232 columns, four rows per staged block; the bed
+     * reads NaN (inactive) outside the array */
     bool ok = true;
     for (int k = 0; k < 2; k++) {
-        ok &= make_map(&d.tm_h[k], d.h[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, T32_LW, T32_LH);
-        ok &= make_map(&d.tm_qx[k], d.qx[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, T32_LW, T32_LH);
-        ok &= make_map(&d.tm_qy[k], d.qy[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, T32_LW, T32_LH);
+        ok &= make_map(&d.tm_h[k], d.h[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, M_BW, M_RB, false);
+        ok &= make_map(&d.tm_qx[k], d.qx[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, M_BW, M_RB, false);
+        ok &= make_map(&d.tm_qy[k], d.qy[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, M_BW, M_RB, false);
     }
-    ok &= make_map(&d.tm_z, dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, T32_LW, T32_LH);
-    ok &= make_map(&d.tm_info, dinfo, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P, NR, T32_LWB, T32_LH);
+    ok &= make_map(&d.tm_z, dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, M_BW, M_RB, true);
     if (!ok) {
         if (err) *err = "cuTensorMapEncodeTiled failed";
         return fail_free(SW2D_ERR_CUDA);
@@ -248,6 +259,7 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     d.P = P;
     d.tiles_x = tx;
     d.tiles_y = ty;
+    d.seg = seg;
     d.outflow_south = in.outflow_south;
     d.series_mode = in.series_mode;
     d.dt_mode = in.dt_mode;
@@ -423,7 +435,7 @@ int Engine32::get_state(int index, double* depth, double* qx, double* qy, std::s
     const int R = S.R, C = S.C, P = S.P;
     std::vector<float> buf((size_t)(R + 1) * (C + 1));
     auto fetch = [&](const float* src, int rows, int cols, double* dst) -> int {
-        ECK(cudaMemcpy2DAsync(buf.data(), (size_t)cols * 4, src + (size_t)T32_H * P + T32_H, (size_t)P * 4,
+        ECK(cudaMemcpy2DAsync(buf.data(), (size_t)cols * 4, src + (size_t)M_H * P + M_H, (size_t)P * 4,
                               (size_t)cols * 4, rows, cudaMemcpyDeviceToHost, stream_));
         ECK(cudaStreamSynchronize(stream_));
         for (size_t k = 0; k < (size_t)rows * cols; k++) dst[k] = buf[k];

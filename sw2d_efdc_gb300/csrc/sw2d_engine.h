@@ -67,6 +67,8 @@ class Engine32 {
     long long last_iters() const { return last_iters_; }
     int nwork() const { return (int)work_.size(); }
     int sync(std::string* err);
+    /* rows per work item of scenarios added from now on (0 = default 128) */
+    void set_segment_rows(int rows) { seg_rows_ = rows; }
 
   private:
     int rebuild(std::string* err);
@@ -88,6 +90,7 @@ class Engine32 {
     cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr;
     double last_ms_ = 0.0;
     long long last_iters_ = 0;
+    int seg_rows_ = 0;
 };
 
 } // namespace sw2d

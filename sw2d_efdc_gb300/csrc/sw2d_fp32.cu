@@ -1,22 +1,26 @@
-/* FP32 precision form of the SW2D step on sm_103a: one fused kernel per
- * iteration.
+/* FP32 precision form of the SW2D step on sm_103a: one row-marching kernel
+ * per iteration.
  *
- * Each CTA owns a 64 x 32 tile of one scenario.  Thread 0 stages the tile
- * with a 4-cell halo (72 x 40) of depth, bed offset, x/y discharges and the
- * info byte into shared memory with five 2-D TMA loads
- * (cp.async.bulk.tensor, one mbarrier); then, all in shared memory:
- *   1. face velocities uu1 = qx/hm, vv1 = qy/hn        (hm_hn, uu1_vv1: SW2D-EFDC.cu:362-452)
- *   2. new x and y face discharges                        (flux: :97-353)
- *   3. provisional depth at t on the tile and a 1-cell ring -> "dry" bytes
- *                                                         (continuity :602-664)
- *   4. outward faces of dry cells closed                   (treat_error :695-725, per face)
- *      final depth at t+dt with a Kahan-compensated increment, written
- *      with the tile's north/west faces; block reductions of the CFL speed
- *      and of the ledger terms.
- * The halo is recomputed instead of exchanged, so an iteration reads every
- * field once from HBM and writes it once (neighbouring tiles' halo reads hit
- * L2).  A second, tiny kernel reduces each scenario's tile partials in a
- * fixed order and prepares the scenario's next iteration (CFL length, rain).
+ * A work item is a 224-column strip x `seg` rows of one scenario, taken by a
+ * CTA of four warps.  Thread 0 streams the strip's rows (232 columns with a
+ * 4-cell halo) of depth, bed offset and x/y discharges into a three-block
+ * ring in shared memory with 2-D TMA loads (cp.async.bulk.tensor, one
+ * mbarrier per block, four rows per block).  Each warp owns 64 staged
+ * columns, two per lane, of which 56 are its output; it marches down the
+ * rows keeping the last four rows of every quantity in registers (vertical
+ * neighbours) and exchanging horizontal neighbours by warp shuffles.  For
+ * each new row L the warp computes
+ *   face velocities of row L                  (hm_hn, uu1_vv1: SW2D-EFDC.cu:362-452)
+ *   x and y face discharges of row L-1         (flux: :97-353)
+ *   provisional depth of row L-2 -> dry flag   (continuity at t: :602-664)
+ *   row L-3: outward faces of dry cells closed (treat_error: :695-725, per face),
+ *            final depth at t+dt with a Kahan-compensated increment,
+ *            written back with its north and west faces.
+ * There is no index arithmetic per cell and no barrier per row; halo rows
+ * and columns are recomputed instead of exchanged, so an iteration reads
+ * every field once from HBM and writes it once.  A second, tiny kernel
+ * reduces each scenario's work-item partials in a fixed order and prepares
+ * the scenario's next iteration (CFL length, rain).
  *
  * Arithmetic is binary32 except the clock, the ledger and the CFL length
  * (binary64).  Gravity uses (h_e - h_w) + (z_e - z_w) with bed offsets from
@@ -29,49 +33,25 @@
 
 namespace sw2d {
 
-#define TC T32_TC
-#define TR T32_TR
-#define LW T32_LW
-#define LH T32_LH
-#define LWB T32_LWB
-#define NT T32_NT
+#define NW M_NW
+#define BW M_BW
+#define RB M_RB
+#define NS M_NS
+#define NT M_NT
 
-/* staged region: local row lr in [0, 40), col lc in [0, 72); global row r0 - 4 + lr */
-#define U_W 68 /* uu1 rows [2, 39), cols [2, 70) */
-#define U_H 37
-#define V_W 69 /* vv1 rows [2, 38), cols [2, 71) */
-#define V_H 36
-#define D_W 66 /* dry rows [3, 37), cols [3, 69) */
-#define D_H 34
-#define FX_W 66 /* x faces rows [3, 38), cols [3, 69) */
-#define FX_H 35
-#define FY_W 67 /* y faces rows [3, 37), cols [3, 70) */
-#define FY_H 34
-
-/* TMA tensor copies need 128-byte aligned shared destinations: the five
- * staged arrays come first, each a multiple of 128 bytes long. */
-struct Smem32 {
-    alignas(128) float h[LH * LW];
-    alignas(128) float z[LH * LW];
-    alignas(128) float qx[LH * LW];
-    alignas(128) float qy[LH * LW];
-    alignas(128) uint8_t info[LH * LWB];
-    alignas(128) float u[U_H * U_W];
-    float v[V_H * V_W];
-    uint8_t dry[D_H * D_W];
+struct SmemM {
+    alignas(128) float stage[NS][4][RB][BW]; /* h, z, qx, qy */
+    unsigned long long bar[NS];
     float ntab[T32_MAXCLASS];
     float dd[9];
-    double red[8][4];
-    float redf[8][2];
-    unsigned long long bar;
+    double red[NW][4];
+    float redf[NW][2];
 };
-static_assert(offsetof(Smem32, h) % 128 == 0 && offsetof(Smem32, z) % 128 == 0, "TMA alignment");
-static_assert(offsetof(Smem32, qx) % 128 == 0 && offsetof(Smem32, qy) % 128 == 0, "TMA alignment");
-static_assert(offsetof(Smem32, info) % 128 == 0, "TMA alignment");
-static_assert(offsetof(Smem32, bar) % 8 == 0, "mbarrier alignment");
-static_assert((LH * LW * 4) % 128 == 0 && (LH * LWB) % 128 == 0, "staged arrays are whole 128-byte lines");
+static_assert(offsetof(SmemM, stage) % 128 == 0, "TMA alignment");
+static_assert((RB * BW * 4) % 128 == 0, "each staged array is whole 128-byte lines");
+static_assert((BW * 4) % 16 == 0, "TMA inner extent must be a multiple of 16 bytes");
 
-size_t fp32_smem_bytes() { return sizeof(Smem32) + 128; }
+size_t fp32_smem_bytes() { return sizeof(SmemM) + 128; }
 
 /* ---------------- TMA and mbarrier (inline PTX) -------------------------- */
 
@@ -107,23 +87,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
         : "memory");
 }
 
-/* Wait for the staged tile with a bounded spin: about 2^31 clock cycles (~1 s).
- * On timeout the scenario's status records it and the CTA gives up. */
-__device__ __forceinline__ bool wait_tile(unsigned long long* bar, Clock32* clk) {
-    long long t0 = clock64();
-    while (!mbar_try_wait(bar, 0)) {
-        if (clock64() - t0 > (1ll << 31)) {
-            if (threadIdx.x == 0) atomicOr(&clk->status, 2);
-            /* second bounded wait for the copies already in flight */
-            long long t1 = clock64();
-            while (!mbar_try_wait(bar, 0) && clock64() - t1 < (1ll << 31)) {
-            }
-            return false;
-        }
-    }
-    return true;
-}
-
 /* ---------------- device helpers ---------------------------------------- */
 
 __device__ __forceinline__ float rpow_manning_f32(float hm) {
@@ -136,20 +99,45 @@ __device__ __forceinline__ float rpow_manning_f32(float hm) {
 __device__ __forceinline__ float fsqrt(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
 
-/* x face between staged cells (lr-1, lc) "w" and (lr, lc) "e" */
-__device__ __forceinline__ float flux_x32(const Smem32& S, const Scn32& P, const Slot32& sl, int lr, int lc,
-                                          int r, int c) {
-    const int e = lr * LW + lc, w = e - LW;
-    const float th = P.th, gg = P.g;
-    const float he = S.h[e], hw = S.h[w];
-    const uint8_t ie = S.info[lr * LWB + lc], iw = S.info[(lr - 1) * LWB + lc];
-    if (r == P.R && P.outflow_south) {
-        if ((iw & SW2D_I_ACTIVE) && hw > th) return 0.5440f * hw * fsqrt(gg * hw);
-        return 0.f;
-    }
-    if (!(ie & iw & SW2D_I_ACTIVE)) return 0.f;
+__device__ __forceinline__ bool is_act(float z) { return z == z; } /* NaN bed offset = inactive */
+
+/* value of the neighbouring column on the left / right for the lane's two
+ * columns (2l, 2l+1) */
+__device__ __forceinline__ float2 left2(float2 v) { return make_float2(__shfl_up_sync(0xffffffffu, v.y, 1), v.x); }
+__device__ __forceinline__ float2 right2(float2 v) { return make_float2(v.y, __shfl_down_sync(0xffffffffu, v.x, 1)); }
+__device__ __forceinline__ int leftbits(int v) { /* bit k = column k; returns neighbours' bits */
+    const int up = __shfl_up_sync(0xffffffffu, v, 1);
+    return ((up >> 1) & 1) | ((v & 1) << 1);
+}
+__device__ __forceinline__ int rightbits(int v) {
+    const int dn = __shfl_down_sync(0xffffffffu, v, 1);
+    return ((v >> 1) & 1) | ((dn & 1) << 1);
+}
+__device__ __forceinline__ float comp(float2 v, int k) { return k ? v.y : v.x; }
+__device__ __forceinline__ void setc(float2& v, int k, float x) {
+    if (k) v.y = x;
+    else v.x = x;
+}
+
+struct FluxIn {
+    float hw, he, zw, ze;          /* cells either side (w = north / s = west) */
+    float nw, ne;                  /* Manning n of the two cells */
+    float u0, uA, uB;              /* velocity on the face, and on the faces before / after along the normal */
+    float q0, qA, qB, qL, qR;      /* old discharge on the face, along the normal, across */
+    float v0, v1, v2, v3;          /* the four cross velocities of the friction and cross convection */
+    bool cross;                    /* cross-convection term present (not column 0 / row 0) */
+};
+
+/* One face of the reference's flux (SW2D-EFDC.cu:110-202 for x, :228-319
+ * for y), in binary32.  For x faces: A = north face, B = south face,
+ * L/R = west/east faces, v0..v3 = vv1 at (r,c), (r,c+1), (r-1,c), (r-1,c+1).
+ * For y faces: A = west face, B = east face, L/R = north/south faces along
+ * x (v11 term), v0..v3 = uu1 at (r,c), (r+1,c), (r,c-1), (r+1,c-1). */
+__device__ __forceinline__ float face_flux(const FluxIn& f, float th, float gg, float dt2, float dt2n, float dt2t,
+                                           bool is_x) {
+    const float he = f.he, hw = f.hw, ze = f.ze, zw = f.zw;
+    if (!is_act(ze) || !is_act(zw)) return 0.f;
     if (!((hw > th) || (he > th))) return 0.f;
-    const float ze = S.z[e], zw = S.z[w];
     const float hhe = he + ze, hhw = hw + zw;
     const float hhep = he - th, hhwp = hw - th;
     if (hhe < zw) return hw > th ? 0.5440f * hw * fsqrt(gg * hw) : 0.f;
@@ -163,327 +151,373 @@ __device__ __forceinline__ float flux_x32(const Smem32& S, const Scn32& P, const
         return 0.f;
     }
     const float hm = 0.5f * (he + hw);
-    const float u13 = gg * hm * sl.dt2dx * ((he - hw) + (ze - zw));
-    const float* U = S.u;
-    const int ui = (lr - 2) * U_W + (lc - 2);
-    const float uc = U[ui], uS = U[ui + U_W], uN = U[ui - U_W];
-    const float u11uur = 0.5f * (uS + uc), u11uul = 0.5f * (uc + uN);
-    const float um0 = S.qx[e], umS = S.qx[e + LW], umN = S.qx[w];
-    const float umr = u11uur * (umS + um0) * 0.5f + fabsf(u11uur) * (um0 - umS) * 0.5f;
-    const float uml = u11uul * (um0 + umN) * 0.5f + fabsf(u11uul) * (umN - um0) * 0.5f;
-    const float u11 = sl.dt2dx * (umr - uml);
-    const float* V = S.v;
-    const int vi = (lr - 2) * V_W + (lc - 2);
-    const float v_e = V[vi], v_e1 = V[vi + 1], v_w = V[vi - V_W], v_w1 = V[vi - V_W + 1];
-    float u12 = 0.f;
-    if (c != 0) {
-        const float u12vvu = 0.5f * (v_e1 + v_w1), u12vvd = 0.5f * (v_e + v_w);
-        const float umE = S.qx[e + 1], umW = S.qx[e - 1];
-        const float umu = u12vvu * (umE + um0) * 0.5f + fabsf(u12vvu) * (um0 - umE) * 0.5f;
-        const float umd = u12vvd * (umW + um0) * 0.5f + fabsf(u12vvd) * (umW - um0) * 0.5f;
-        u12 = sl.dt2dy * (umu - umd);
+    const float grav = gg * hm * dt2n * ((he - hw) + (ze - zw));
+    /* convection along the normal */
+    const float aB = 0.5f * (f.uB + f.u0), aA = 0.5f * (f.u0 + f.uA);
+    const float cB = aB * (f.qB + f.q0) * 0.5f + fabsf(aB) * (f.q0 - f.qB) * 0.5f;
+    const float cA = aA * (f.q0 + f.qA) * 0.5f + fabsf(aA) * (f.qA - f.q0) * 0.5f;
+    const float along = dt2n * (cB - cA);
+    /* convection across */
+    float across = 0.f;
+    if (f.cross) {
+        (void)is_x;
+        const float wu = 0.5f * (f.v1 + f.v3), wd = 0.5f * (f.v0 + f.v2);
+        const float cu = wu * (f.qR + f.q0) * 0.5f + fabsf(wu) * (f.q0 - f.qR) * 0.5f;
+        const float cd = wd * (f.qL + f.q0) * 0.5f + fabsf(wd) * (f.qL - f.q0) * 0.5f;
+        across = dt2t * (cu - cd);
     }
-    const float vva = 0.25f * (v_e + v_e1 + v_w + v_w1);
-    const float sqx = fsqrt(uc * uc + vva * vva);
+    const float vt = 0.25f * (f.v0 + f.v1 + f.v2 + f.v3);
+    const float sq = fsqrt(f.u0 * f.u0 + vt * vt);
     float ram = 0.f;
     if (hm > th) {
-        const float nf = 0.5f * (S.ntab[ie >> 1] + S.ntab[iw >> 1]);
-        ram = gg * nf * nf * sqx * rpow_manning_f32(hm);
+        const float nf = 0.5f * (f.ne + f.nw);
+        ram = gg * nf * nf * sq * rpow_manning_f32(hm);
     }
-    const float a = sl.dt2 * ram * 0.5f;
-    return fdiv((1.f - a) * um0 + (-u11 - u12 - u13), 1.f + a);
+    const float a = dt2 * ram * 0.5f;
+    return fdiv((1.f - a) * f.q0 + (-along - across - grav), 1.f + a);
 }
 
-/* y face between staged cells (lr, lc-1) "s" and (lr, lc) "n" */
-__device__ __forceinline__ float flux_y32(const Smem32& S, const Scn32& P, const Slot32& sl, int lr, int lc,
-                                          int r) {
-    const int n = lr * LW + lc, so = n - 1;
-    const float th = P.th, gg = P.g;
-    const uint8_t in = S.info[lr * LWB + lc], is = S.info[lr * LWB + lc - 1];
-    if (!(in & is & SW2D_I_ACTIVE)) return 0.f;
-    const float hn = S.h[n], hs = S.h[so];
-    if (!((hs > th) || (hn > th))) return 0.f;
-    const float zn = S.z[n], zs = S.z[so];
-    const float hhn = hn + zn, hhs = hs + zs;
-    const float hhnp = hn - th, hhsp = hs - th;
-    if (hhn < zs) return hs > th ? 0.5440f * hs * fsqrt(gg * hs) : 0.f;
-    if (hhs < zn) return hn > th ? -0.544f * hn * fsqrt(gg * hn) : 0.f;
-    if (hhnp * hhsp < 0.f) {
-        if ((hn > 0.f) || (hs > 0.f)) {
-            const float sg = copysignf(1.f, hhnp - hhsp);
-            const float hh3 = fmaxf(hhn, hhs) - fmaxf(zn, zs);
-            return -sg * 0.350f * hh3 * fsqrt(2.f * gg * hh3);
-        }
-        return 0.f;
-    }
-    const float hnf = 0.5f * (hn + hs);
-    const float v13 = gg * hnf * sl.dt2dy * ((hn - hs) + (zn - zs));
-    const float vn0 = S.qy[n];
-    const float* U = S.u;
-    const int ui = (lr - 2) * U_W + (lc - 2);
-    const float ua = U[ui], ub = U[ui + U_W], uc = U[ui - 1], ud = U[ui + U_W - 1];
-    float v11 = 0.f;
-    if (r != 0) {
-        const float v11uur = 0.5f * (ub + ud), v11uul = 0.5f * (ua + uc);
-        const float vS = S.qy[n + LW], vN = S.qy[n - LW];
-        const float vnr = v11uur * (vS + vn0) * 0.5f + fabsf(v11uur) * (vn0 - vS) * 0.5f;
-        const float vnl = v11uul * (vn0 + vN) * 0.5f + fabsf(v11uul) * (vN - vn0) * 0.5f;
-        v11 = sl.dt2dx * (vnr - vnl);
-    }
-    const float* V = S.v;
-    const int vi = (lr - 2) * V_W + (lc - 2);
-    const float vc = V[vi];
-    const float v12vvu = 0.5f * (V[vi + 1] + vc), v12vvd = 0.5f * (vc + V[vi - 1]);
-    const float vE = S.qy[n + 1], vW = S.qy[n - 1];
-    const float vnu = v12vvu * (vE + vn0) * 0.5f + fabsf(v12vvu) * (vn0 - vE) * 0.5f;
-    const float vnd = v12vvd * (vW + vn0) * 0.5f + fabsf(v12vvd) * (vW - vn0) * 0.5f;
-    const float v12 = sl.dt2dy * (vnu - vnd);
-    const float uua = 0.25f * (ua + ub + uc + ud);
-    const float sqy = fsqrt(uua * uua + vc * vc);
-    float ram = 0.f;
-    if (hnf > th) {
-        const float nf = 0.5f * (S.ntab[in >> 1] + S.ntab[is >> 1]);
-        ram = gg * nf * nf * sqy * rpow_manning_f32(hnf);
-    }
-    const float a = sl.dt2 * ram * 0.5f;
-    return fdiv((1.f - a) * vn0 + (-v11 - v12 - v13), 1.f + a);
-}
+/* ---------------- the row-marching step ---------------------------------- */
 
-__device__ __forceinline__ float pct_of(const Scn32& P, float ho) {
-    return ho > P.ev_wl_min ? P.pct_lake : P.pct_land;
-}
-
-/* ---------------- the fused step ---------------------------------------- */
-
-__global__ void __launch_bounds__(NT, 3) k32_step(const Scn32* __restrict__ scns, const int4* __restrict__ work,
-                                                  Part32* __restrict__ part) {
+__global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scns, const int4* __restrict__ work,
+                                                   Part32* __restrict__ part) {
     extern __shared__ unsigned char smem_raw[];
-    Smem32& S = *reinterpret_cast<Smem32*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    const int tid = threadIdx.x;
+    SmemM& S = *reinterpret_cast<SmemM*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int4 w = work[blockIdx.x];
     const Scn32& P = scns[w.x];
     Clock32* clk = P.clk;
     const Slot32 sl = clk->slot;
     if (!sl.active) {
         if (tid == 0) {
-            Part32 z = {};
-            part[blockIdx.x] = z;
+            Part32 zp = {};
+            part[blockIdx.x] = zp;
         }
         return;
     }
     const int cur = sl.cur, nxt = cur ^ 1;
-    const int tx = w.y, ty = w.z;
-    const int c0 = tx * TC, r0 = ty * TR;
+    const int R = P.R, C = P.C, Pp = P.P;
+    const int strip = w.y, seg = w.z;
+    const int c0 = strip * M_CW;             /* first output column of the strip */
+    const int rs = seg * P.seg, re = min(rs + P.seg, R);
+    const int Ls = rs - 3;                   /* first staged row */
+    const int nblk = (re - rs + 6 + RB - 1) / RB;
 
-    /* self-check of the staging layout: a misaligned TMA destination would
-     * fault, so record it and skip the tile instead */
-    if (((smem_addr(S.h) | smem_addr(S.z) | smem_addr(S.qx) | smem_addr(S.qy) | smem_addr(S.info)) & 127u) != 0u) {
+    if ((smem_addr(&S.stage[0][0][0][0]) & 127u) != 0u) {
         if (tid == 0) atomicOr(&clk->status, 4);
         return;
     }
     if (tid == 0) {
-        mbar_init(&S.bar, 1);
+        for (int k = 0; k < NS; k++) mbar_init(&S.bar[k], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const unsigned bytes = 4u * LH * LW * sizeof(float) + LH * LWB;
-        mbar_arrive_expect_tx(&S.bar, bytes);
-        /* staged origin (r0 - 4, c0 - 4) is padded coordinate (c0, r0) */
-        tma_load_2d(S.h, &P.tm_h[cur], c0, r0, &S.bar);
-        tma_load_2d(S.z, &P.tm_z, c0, r0, &S.bar);
-        tma_load_2d(S.qx, &P.tm_qx[cur], c0, r0, &S.bar);
-        tma_load_2d(S.qy, &P.tm_qy[cur], c0, r0, &S.bar);
-        tma_load_2d(S.info, &P.tm_info, c0, r0, &S.bar);
     }
     if (tid < T32_MAXCLASS) S.ntab[tid] = P.ntab[tid];
     if (tid < 9) {
         const int dy = tid / 3 - 1, dx = tid % 3 - 1;
-        const int ny = ty + dy, nx = tx + dx;
+        const int ny = seg + dy, nx = strip + dx;
         float d = 0.f;
         if (ny >= 0 && ny < P.tiles_y && nx >= 0 && nx < P.tiles_x)
-            d = P.datum[ny * P.tiles_x + nx] - P.datum[ty * P.tiles_x + tx];
+            d = P.datum[ny * P.tiles_x + nx] - P.datum[seg * P.tiles_x + strip];
         S.dd[tid] = d;
     }
-    if (!wait_tile(&S.bar, clk)) return;
     __syncthreads();
-
-    /* bed offsets of halo cells from the neighbouring tiles' datum to ours */
-    for (int k = tid; k < LH * LW; k += NT) {
-        const int lr = k / LW, lc = k - lr * LW;
-        const int dy = lr < T32_H ? 0 : (lr >= T32_H + TR ? 2 : 1);
-        const int dx = lc < T32_H ? 0 : (lc >= T32_H + TC ? 2 : 1);
-        if (dy != 1 || dx != 1) S.z[k] += S.dd[dy * 3 + dx];
+    const unsigned blk_bytes = 4u * RB * BW * 4u;
+    if (tid == 0) {
+        for (int b = 0; b < NS && b < nblk; b++) {
+            mbar_arrive_expect_tx(&S.bar[b], blk_bytes);
+            const int y = Ls + b * RB + M_H; /* padded row of the block's first row */
+            tma_load_2d(&S.stage[b][0][0][0], &P.tm_h[cur], c0, y, &S.bar[b]);
+            tma_load_2d(&S.stage[b][1][0][0], &P.tm_z, c0, y, &S.bar[b]);
+            tma_load_2d(&S.stage[b][2][0][0], &P.tm_qx[cur], c0, y, &S.bar[b]);
+            tma_load_2d(&S.stage[b][3][0][0], &P.tm_qy[cur], c0, y, &S.bar[b]);
+        }
     }
 
-    /* 1. face velocities, and the CFL face speeds of the tile's own faces
-     *    (north and west faces of its cells between two active cells) */
-    const float th = P.th;
-    float sx = 0.f, sy = 0.f;
-    for (int k = tid; k < U_H * U_W; k += NT) {
-        const int lr = 2 + k / U_W, lc = 2 + k % U_W;
-        const int r = r0 - T32_H + lr;
-        const int i = lr * LW + lc;
-        const float hm = (r == P.R) ? S.h[i - LW] : 0.5f * (S.h[i] + S.h[i - LW]);
-        const float q = S.qx[i];
-        const float u = (hm >= th && q != 0.f) ? fdiv(q, hm) : 0.f;
-        S.u[k] = u;
-        if (lr >= T32_H && lr < T32_H + TR && lc >= T32_H && lc < T32_H + TC && hm >= th &&
-            (S.info[lr * LWB + lc] & S.info[(lr - 1) * LWB + lc] & SW2D_I_ACTIVE))
-            sx = fmaxf(sx, (fabsf(u) + fsqrt(P.g * hm)) * P.rdx);
-    }
-    for (int k = tid; k < V_H * V_W; k += NT) {
-        const int lr = 2 + k / V_W, lc = 2 + k % V_W;
-        const int i = lr * LW + lc;
-        const float hn = 0.5f * (S.h[i] + S.h[i - 1]);
-        const float q = S.qy[i];
-        const float v = (hn >= th && q != 0.f) ? fdiv(q, hn) : 0.f;
-        S.v[k] = v;
-        if (lr >= T32_H && lr < T32_H + TR && lc >= T32_H && lc < T32_H + TC && hn >= th &&
-            (S.info[lr * LWB + lc] & S.info[lr * LWB + lc - 1] & SW2D_I_ACTIVE))
-            sy = fmaxf(sy, (fabsf(v) + fsqrt(P.g * hn)) * P.rdy);
-    }
-    __syncthreads();
+    /* lane geometry: staged columns sc, sc+1; global columns cg, cg+1 */
+    const int sc = warp * M_SW + 2 * lane;
+    const int cg = c0 - M_H + sc;
+    const bool own0 = (lane >= 2 && lane < 30) && cg < C;
+    const bool own1 = (lane >= 2 && lane < 30) && cg + 1 < C;
+    const int creg0 = sc < M_H ? 0 : (sc >= M_H + M_CW ? 2 : 1);
+    const int creg1 = sc + 1 < M_H ? 0 : (sc + 1 >= M_H + M_CW ? 2 : 1);
+    /* datum shifts of the lane's two columns for rows above / inside / below the segment */
+    const float dzt0 = S.dd[creg0], dzm0 = S.dd[3 + creg0], dzb0 = S.dd[6 + creg0];
+    const float dzt1 = S.dd[creg1], dzm1 = S.dd[3 + creg1], dzb1 = S.dd[6 + creg1];
+    const float th = P.th, gg = P.g, rdx = P.rdx, rdy = P.rdy;
+    const float dt2 = sl.dt2, dt2dx = sl.dt2dx, dt2dy = sl.dt2dy;
+    const bool has_cls = P.cls != nullptr, has_rw = P.rainw != nullptr;
+    const float n_uni = S.ntab[0];
 
-    /* 2a. x faces (need qx as the old discharge, so results wait in registers) */
-    constexpr int NFX = (FX_H * FX_W + NT - 1) / NT;
-    float fx[NFX];
+    /* register windows, slot = row & 3 relative to Ls */
+    float2 H[4], Z[4], QX[4], QY[4], U[4], V[4], FX[4], FY[4];
+    float2 HL[4], ZL[4], UL[4], VR[4], FYR[4], RW[4], NN[4], NL[4];
+    int DRY[4];
 #pragma unroll
-    for (int j = 0; j < NFX; j++) {
-        const int k = tid + j * NT;
-        fx[j] = 0.f;
-        if (k < FX_H * FX_W) {
-            const int lr = 3 + k / FX_W, lc = 3 + k % FX_W;
-            fx[j] = flux_x32(S, P, sl, lr, lc, r0 - T32_H + lr, c0 - T32_H + lc);
-        }
+    for (int k = 0; k < 4; k++) {
+        H[k] = Z[k] = QX[k] = QY[k] = U[k] = V[k] = FX[k] = FY[k] = make_float2(0.f, 0.f);
+        HL[k] = ZL[k] = UL[k] = VR[k] = FYR[k] = NN[k] = NL[k] = make_float2(0.f, 0.f);
+        RW[k] = make_float2(1.f, 1.f);
+        DRY[k] = 0;
     }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < NFX; j++) {
-        const int k = tid + j * NT;
-        if (k < FX_H * FX_W) {
-            const int lr = 3 + k / FX_W, lc = 3 + k % FX_W;
-            S.qx[lr * LW + lc] = fx[j];
-        }
-    }
-    /* 2b. y faces */
-    constexpr int NFY = (FY_H * FY_W + NT - 1) / NT;
-    float fy[NFY];
-#pragma unroll
-    for (int j = 0; j < NFY; j++) {
-        const int k = tid + j * NT;
-        fy[j] = 0.f;
-        if (k < FY_H * FY_W) {
-            const int lr = 3 + k / FY_W, lc = 3 + k % FY_W;
-            fy[j] = flux_y32(S, P, sl, lr, lc, r0 - T32_H + lr);
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < NFY; j++) {
-        const int k = tid + j * NT;
-        if (k < FY_H * FY_W) {
-            const int lr = 3 + k / FY_W, lc = 3 + k % FY_W;
-            S.qy[lr * LW + lc] = fy[j];
-        }
-    }
-    __syncthreads();
+    float clamp = 0.f, qout = 0.f, rainacc = 0.f, evc = 0.f, sxm = 0.f, sym = 0.f;
 
-    /* 3. provisional depth at t on the tile and its ring */
-    const float rdx = P.rdx, rdy = P.rdy;
-    for (int k = tid; k < D_H * D_W; k += NT) {
-        const int lr = 3 + k / D_W, lc = 3 + k % D_W;
-        const int i = lr * LW + lc;
-        const uint8_t inf = S.info[lr * LWB + lc];
-        uint8_t dry = 0;
-        if (inf & SW2D_I_ACTIVE) {
-            const float ho = S.h[i];
-            float rr = sl.rr1;
-            if (P.rainw) rr *= P.rainw[(size_t)(r0 + lr) * P.P + (c0 + lc)];
-            const float ev = ho > P.ev_wl_min ? sl.ev1 : 0.f;
-            const float hs = ho - sl.dt2 * ((S.qx[i + LW] - S.qx[i]) * rdx + (S.qy[i + 1] - S.qy[i]) * rdy -
-                                            rr * pct_of(P, ho) + ev);
-            dry = hs < th;
-        }
-        S.dry[k] = dry;
-    }
-    __syncthreads();
-
-    /* 4. close outward faces of dry cells, final depth, write back */
-    float clamp = 0.f, qout = 0.f, rain = 0.f, evc = 0.f;
-    const int lc = T32_H + (tid % TC);
-    const int c = c0 + (tid % TC);
-#pragma unroll 2
-    for (int j = 0; j < TR * TC / NT; j++) {
-        const int lr = T32_H + tid / TC + j * (NT / TC);
-        const int r = r0 + (lr - T32_H);
-        if (r >= P.R || c >= P.C) continue;
-        const int i = lr * LW + lc;
-        const int di = (lr - 3) * D_W + (lc - 3);
-        const uint8_t dc = S.dry[di];
-        float fN = S.qx[i], fS = S.qx[i + LW], fW = S.qy[i], fE = S.qy[i + 1];
-        if ((fN > 0.f && S.dry[di - D_W]) || (fN < 0.f && dc)) fN = 0.f;
-        if ((fS > 0.f && dc) || (fS < 0.f && S.dry[di + D_W])) fS = 0.f;
-        if ((fW > 0.f && S.dry[di - 1]) || (fW < 0.f && dc)) fW = 0.f;
-        if ((fE > 0.f && dc) || (fE < 0.f && S.dry[di + 1])) fE = 0.f;
-        const size_t g = (size_t)(r + T32_H) * P.P + (c + T32_H);
-        const uint8_t inf = S.info[lr * LWB + lc];
-        float hn = 0.f, kc = 0.f;
-        if (inf & SW2D_I_ACTIVE) {
-            const float ho = S.h[i];
-            float wgt = P.rainw ? P.rainw[g] : 1.f;
-            const float pct = pct_of(P, ho);
-            const float ev = ho > P.ev_wl_min ? sl.ev2 : 0.f;
-            const float dh = -sl.dt2 * ((fS - fN) * rdx + (fE - fW) * rdy - sl.rr2 * wgt * pct + ev);
-            /* Kahan: the increment is small against the depth */
-            const float y = dh - P.kc[g];
-            const float t = ho + y;
-            kc = (t - ho) - y;
-            hn = t;
-            if (hn < 0.f) {
-                clamp -= hn;
-                hn = 0.f;
-                kc = 0.f;
+    for (int b = 0; b < nblk; b++) {
+        const int st = b % NS;
+        /* bounded wait for the block (about 2^31 cycles); the CTA agrees on
+         * the outcome so that no warp is left waiting at a barrier */
+        {
+            const unsigned par = (unsigned)((b / NS) & 1);
+            long long t0 = clock64();
+            bool ok = true;
+            while (!mbar_try_wait(&S.bar[st], par)) {
+                if (clock64() - t0 > (1ll << 31)) {
+                    ok = false;
+                    break;
+                }
             }
-            if (P.ledger_cells) {
-                rain += wgt * pct;
-                evc += ho > P.ev_wl_min ? 1.f : 0.f;
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) atomicOr(&clk->status, 2);
+                return;
             }
         }
-        P.h[nxt][g] = hn;
-        P.kc[g] = kc;
-        P.qx[nxt][g] = fN;
-        P.qy[nxt][g] = fW;
-        if (r == P.R - 1) {
-            P.qx[nxt][g + P.P] = fS;
-            qout += fS;
+        const float* sh = &S.stage[st][0][0][0];
+        const float* sz = &S.stage[st][1][0][0];
+        const float* sqx = &S.stage[st][2][0][0];
+        const float* sqy = &S.stage[st][3][0][0];
+#pragma unroll
+        for (int j = 0; j < RB; j++) {
+            const int L = Ls + b * RB + j;
+            const int s0 = j & 3, s1 = (j + 3) & 3, s2 = (j + 2) & 3, s3 = (j + 1) & 3; /* L, L-1, L-2, L-3 */
+            /* ---- load row L ---- */
+            H[s0] = *reinterpret_cast<const float2*>(sh + j * BW + sc);
+            float2 zz = *reinterpret_cast<const float2*>(sz + j * BW + sc);
+            zz.x += L < rs ? dzt0 : (L >= re ? dzb0 : dzm0);
+            zz.y += L < rs ? dzt1 : (L >= re ? dzb1 : dzm1);
+            Z[s0] = zz;
+            QX[s0] = *reinterpret_cast<const float2*>(sqx + j * BW + sc);
+            QY[s0] = *reinterpret_cast<const float2*>(sqy + j * BW + sc);
+            if (has_cls) {
+                const size_t g = (size_t)(L + M_H) * Pp + (cg + M_H);
+                float2 nn;
+                if (L >= -M_H && L < R + M_H && cg + M_H >= 0 && cg + M_H + 1 < Pp) {
+                    const uchar2 cc = *reinterpret_cast<const uchar2*>(P.cls + g);
+                    nn = make_float2(S.ntab[cc.x & 63], S.ntab[cc.y & 63]);
+                } else {
+                    nn = make_float2(n_uni, n_uni);
+                }
+                NN[s0] = nn;
+                NL[s0] = left2(nn);
+            } else {
+                NN[s0] = NL[s0] = make_float2(n_uni, n_uni);
+            }
+            if (has_rw) {
+                const size_t g = (size_t)(L + M_H) * Pp + (cg + M_H);
+                RW[s0] = (L >= -M_H && L < R + M_H && cg + M_H >= 0 && cg + M_H + 1 < Pp)
+                             ? *reinterpret_cast<const float2*>(P.rainw + g)
+                             : make_float2(1.f, 1.f);
+            }
+            /* ---- face velocities of row L; CFL face speeds of owned faces ---- */
+            HL[s0] = left2(H[s0]);
+            ZL[s0] = left2(Z[s0]);
+            const bool rowown = (L >= rs && L < re);
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                const float hLk = comp(H[s0], k), hUk = comp(H[s1], k);
+                const float hm = (L == R) ? hUk : 0.5f * (hLk + hUk);
+                const float q = comp(QX[s0], k);
+                const float u = (hm >= th && q != 0.f) ? fdiv(q, hm) : 0.f;
+                setc(U[s0], k, u);
+                const float hn = 0.5f * (hLk + comp(HL[s0], k));
+                const float qy = comp(QY[s0], k);
+                const float v = (hn >= th && qy != 0.f) ? fdiv(qy, hn) : 0.f;
+                setc(V[s0], k, v);
+                const bool own = k ? own1 : own0;
+                if (rowown && own) {
+                    if (hm >= th && is_act(comp(Z[s0], k)) && is_act(comp(Z[s1], k)))
+                        sxm = fmaxf(sxm, (fabsf(u) + fsqrt(gg * hm)) * rdx);
+                    if (hn >= th && is_act(comp(Z[s0], k)) && is_act(comp(ZL[s0], k)))
+                        sym = fmaxf(sym, (fabsf(v) + fsqrt(gg * hn)) * rdy);
+                }
+            }
+            UL[s0] = left2(U[s0]);
+            VR[s0] = right2(V[s0]);
+            /* ---- face discharges of row L-1 ---- */
+            {
+                const float2 qxl = left2(QX[s1]), qxr = right2(QX[s1]);
+                const float2 qyl = left2(QY[s1]), qyr = right2(QY[s1]);
+                const float2 vl = left2(V[s1]);
+                const int rf = L - 1;
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const int c = cg + k;
+                    FluxIn fx;
+                    fx.hw = comp(H[s2], k);
+                    fx.he = comp(H[s1], k);
+                    fx.zw = comp(Z[s2], k);
+                    fx.ze = comp(Z[s1], k);
+                    fx.nw = comp(NN[s2], k);
+                    fx.ne = comp(NN[s1], k);
+                    fx.u0 = comp(U[s1], k);
+                    fx.uA = comp(U[s2], k);
+                    fx.uB = comp(U[s0], k);
+                    fx.q0 = comp(QX[s1], k);
+                    fx.qA = comp(QX[s2], k);
+                    fx.qB = comp(QX[s0], k);
+                    fx.qL = comp(qxl, k);
+                    fx.qR = comp(qxr, k);
+                    fx.v0 = comp(V[s1], k);
+                    fx.v1 = comp(VR[s1], k);
+                    fx.v2 = comp(V[s2], k);
+                    fx.v3 = comp(VR[s2], k);
+                    fx.cross = (c != 0);
+                    float F;
+                    if (rf == R && P.outflow_south) {
+                        const float hwk = fx.hw;
+                        F = (is_act(fx.zw) && hwk > th) ? 0.5440f * hwk * fsqrt(gg * hwk) : 0.f;
+                    } else {
+                        F = face_flux(fx, th, gg, dt2, dt2dx, dt2dy, true);
+                    }
+                    setc(FX[s1], k, F);
+                    FluxIn fy;
+                    fy.hw = comp(HL[s1], k);
+                    fy.he = comp(H[s1], k);
+                    fy.zw = comp(ZL[s1], k);
+                    fy.ze = comp(Z[s1], k);
+                    fy.nw = comp(NL[s1], k);
+                    fy.ne = comp(NN[s1], k);
+                    fy.u0 = comp(V[s1], k);
+                    fy.uA = comp(vl, k);
+                    fy.uB = comp(VR[s1], k);
+                    fy.q0 = comp(QY[s1], k);
+                    fy.qA = comp(qyl, k);
+                    fy.qB = comp(qyr, k);
+                    fy.qL = comp(QY[s2], k);
+                    fy.qR = comp(QY[s0], k);
+                    fy.v0 = comp(U[s1], k);
+                    fy.v1 = comp(U[s0], k);
+                    fy.v2 = comp(UL[s1], k);
+                    fy.v3 = comp(UL[s0], k);
+                    fy.cross = (rf != 0);
+                    setc(FY[s1], k, face_flux(fy, th, gg, dt2, dt2dy, dt2dx, false));
+                }
+            }
+            /* ---- provisional depth of row L-2 -> dry flags ---- */
+            FYR[s2] = right2(FY[s2]);
+            {
+                int dry = 0;
+#pragma unroll
+                for (int k = 0; k < 2; k++) {
+                    const float ho = comp(H[s2], k);
+                    if (is_act(comp(Z[s2], k))) {
+                        const float pct = ho > P.ev_wl_min ? P.pct_lake : P.pct_land;
+                        const float ev = ho > P.ev_wl_min ? sl.ev1 : 0.f;
+                        const float hs = ho - dt2 * ((comp(FX[s1], k) - comp(FX[s2], k)) * rdx +
+                                                     (comp(FYR[s2], k) - comp(FY[s2], k)) * rdy -
+                                                     sl.rr1 * comp(RW[s2], k) * pct + ev);
+                        dry |= (hs < th) ? (1 << k) : 0;
+                    }
+                }
+                DRY[s2] = dry;
+            }
+            /* ---- final depth of row L-3 ---- */
+            {
+                const int r = L - 3;
+                const int dc = DRY[s3], dN = DRY[s0], dS = DRY[s2];
+                const int dW = leftbits(dc), dE = rightbits(dc);
+                if (r >= rs && r < re) {
+                    const size_t g = (size_t)(r + M_H) * Pp + (cg + M_H);
+                    float2 kcv = make_float2(0.f, 0.f);
+                    if (own0 || own1) kcv = own1 ? *reinterpret_cast<const float2*>(P.kc + g)
+                                                 : make_float2(P.kc[g], 0.f);
+                    float2 hout, kout, fNo, fWo, fSo;
+#pragma unroll
+                    for (int k = 0; k < 2; k++) {
+                        float fN = comp(FX[s3], k), fS = comp(FX[s2], k), fW = comp(FY[s3], k), fE = comp(FYR[s3], k);
+                        const int bc = (dc >> k) & 1;
+                        if ((fN > 0.f && ((dN >> k) & 1)) || (fN < 0.f && bc)) fN = 0.f;
+                        if ((fS > 0.f && bc) || (fS < 0.f && ((dS >> k) & 1))) fS = 0.f;
+                        if ((fW > 0.f && ((dW >> k) & 1)) || (fW < 0.f && bc)) fW = 0.f;
+                        if ((fE > 0.f && bc) || (fE < 0.f && ((dE >> k) & 1))) fE = 0.f;
+                        float hn = 0.f, kc = 0.f;
+                        const bool own = k ? own1 : own0;
+                        if (is_act(comp(Z[s3], k))) {
+                            const float ho = comp(H[s3], k);
+                            const float wgt = comp(RW[s3], k);
+                            const float pct = ho > P.ev_wl_min ? P.pct_lake : P.pct_land;
+                            const float ev = ho > P.ev_wl_min ? sl.ev2 : 0.f;
+                            const float dh = -dt2 * ((fS - fN) * rdx + (fE - fW) * rdy - sl.rr2 * wgt * pct + ev);
+                            const float y = dh - comp(kcv, k);
+                            const float t = ho + y;
+                            kc = (t - ho) - y;
+                            hn = t;
+                            if (hn < 0.f) {
+                                if (own) clamp -= hn;
+                                hn = 0.f;
+                                kc = 0.f;
+                            }
+                            if (own && P.ledger_cells) {
+                                rainacc += wgt * pct;
+                                evc += ho > P.ev_wl_min ? 1.f : 0.f;
+                            }
+                        }
+                        setc(hout, k, hn);
+                        setc(kout, k, kc);
+                        setc(fNo, k, fN);
+                        setc(fWo, k, fW);
+                        setc(fSo, k, fS);
+                        if (own && r == R - 1) qout += fS;
+                    }
+                    if (own0 && own1) {
+                        *reinterpret_cast<float2*>(P.h[nxt] + g) = hout;
+                        *reinterpret_cast<float2*>(P.kc + g) = kout;
+                        *reinterpret_cast<float2*>(P.qx[nxt] + g) = fNo;
+                        *reinterpret_cast<float2*>(P.qy[nxt] + g) = fWo;
+                        if (r == R - 1) *reinterpret_cast<float2*>(P.qx[nxt] + g + Pp) = fSo;
+                    } else if (own0) {
+                        P.h[nxt][g] = hout.x;
+                        P.kc[g] = kout.x;
+                        P.qx[nxt][g] = fNo.x;
+                        P.qy[nxt][g] = fWo.x;
+                        if (r == R - 1) P.qx[nxt][g + Pp] = fSo.x;
+                    }
+                }
+            }
+        }
+        __syncthreads(); /* every warp is done with block b */
+        if (tid == 0 && b + NS < nblk) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive_expect_tx(&S.bar[st], blk_bytes);
+            const int y = Ls + (b + NS) * RB + M_H;
+            tma_load_2d(&S.stage[st][0][0][0], &P.tm_h[cur], c0, y, &S.bar[st]);
+            tma_load_2d(&S.stage[st][1][0][0], &P.tm_z, c0, y, &S.bar[st]);
+            tma_load_2d(&S.stage[st][2][0][0], &P.tm_qx[cur], c0, y, &S.bar[st]);
+            tma_load_2d(&S.stage[st][3][0][0], &P.tm_qy[cur], c0, y, &S.bar[st]);
         }
     }
 
     /* block reductions: warp sums in binary32, across warps in binary64 */
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        sx = fmaxf(sx, __shfl_xor_sync(0xffffffffu, sx, o));
-        sy = fmaxf(sy, __shfl_xor_sync(0xffffffffu, sy, o));
+        sxm = fmaxf(sxm, __shfl_xor_sync(0xffffffffu, sxm, o));
+        sym = fmaxf(sym, __shfl_xor_sync(0xffffffffu, sym, o));
         clamp += __shfl_xor_sync(0xffffffffu, clamp, o);
         qout += __shfl_xor_sync(0xffffffffu, qout, o);
-        rain += __shfl_xor_sync(0xffffffffu, rain, o);
+        rainacc += __shfl_xor_sync(0xffffffffu, rainacc, o);
         evc += __shfl_xor_sync(0xffffffffu, evc, o);
     }
-    const int warp = tid >> 5, lane = tid & 31;
     if (lane == 0) {
         S.red[warp][0] = clamp;
         S.red[warp][1] = qout;
-        S.red[warp][2] = rain;
+        S.red[warp][2] = rainacc;
         S.red[warp][3] = evc;
-        S.redf[warp][0] = sx;
-        S.redf[warp][1] = sy;
+        S.redf[warp][0] = sxm;
+        S.redf[warp][1] = sym;
     }
     __syncthreads();
     if (tid == 0) {
         Part32 pr = {};
         float mx = 0.f, my = 0.f;
-        for (int k = 0; k < NT / 32; k++) {
+        for (int k = 0; k < NW; k++) {
             pr.clamp += S.red[k][0];
             pr.qout += S.red[k][1];
             pr.rain += S.red[k][2];
@@ -622,16 +656,16 @@ __global__ void k32_volume(const Scn32* __restrict__ scns, int iscn, double* out
     float sx = 0.f, sy = 0.f;
     for (long long k = threadIdx.x; k < (long long)P.R * P.C; k += blockDim.x) {
         const int r = (int)(k / P.C), c = (int)(k % P.C);
-        const size_t g = (size_t)(r + T32_H) * P.P + (c + T32_H);
-        if (!(P.info[g] & SW2D_I_ACTIVE)) continue;
+        const size_t g = (size_t)(r + M_H) * P.P + (c + M_H);
+        if (!is_act(P.z[g])) continue;
         const float hh = P.h[cur][g];
         vol += (double)hh - (double)P.kc[g];
-        if (r > 0 && (P.info[g - P.P] & SW2D_I_ACTIVE)) {
+        if (r > 0 && is_act(P.z[g - P.P])) {
             const float hm = 0.5f * (hh + P.h[cur][g - P.P]);
             const float q = P.qx[cur][g];
             if (hm >= th) sx = fmaxf(sx, (fabsf(q != 0.f ? q / hm : 0.f) + fsqrt(P.g * hm)) * P.rdx);
         }
-        if (c > 0 && (P.info[g - 1] & SW2D_I_ACTIVE)) {
+        if (c > 0 && is_act(P.z[g - 1])) {
             const float hn = 0.5f * (hh + P.h[cur][g - 1]);
             const float q = P.qy[cur][g];
             if (hn >= th) sy = fmaxf(sy, (fabsf(q != 0.f ? q / hn : 0.f) + fsqrt(P.g * hn)) * P.rdy);
@@ -658,13 +692,13 @@ __global__ void k32_volume(const Scn32* __restrict__ scns, int iscn, double* out
 }
 
 int fp32_configure_kernels() {
-    cudaError_t e = cudaFuncSetAttribute(k32_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fp32_smem_bytes());
+    cudaError_t e = cudaFuncSetAttribute(k32_march, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fp32_smem_bytes());
     return e == cudaSuccess ? 0 : -1;
 }
 
 void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, int nwork, Part32* d_part,
                            cudaStream_t s) {
-    if (nwork > 0) k32_step<<<nwork, NT, fp32_smem_bytes(), s>>>(d_scn, d_work, d_part);
+    if (nwork > 0) k32_march<<<nwork, NT, fp32_smem_bytes(), s>>>(d_scn, d_work, d_part);
     k32_finalize<<<(nscn + 3) / 4, 128, 0, s>>>(d_scn, nscn, d_part);
 }
 

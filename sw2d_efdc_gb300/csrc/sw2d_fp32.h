@@ -1,15 +1,17 @@
 /* FP32 precision form of the SW2D step: device-side structures shared by the
- * fused tile kernel (sw2d_fp32.cu) and the scenario engine (sw2d_engine.cu).
+ * row-marching kernel (sw2d_fp32.cu) and the scenario engine (sw2d_engine.cu).
  *
  * One kernel serves the single-raster, batched and served forms: its work
- * list holds (scenario, tile) pairs and every scenario has its own
- * descriptor, clock, iteration length and forcing.
+ * list holds (scenario, column strip, row segment) triples and every
+ * scenario has its own descriptor, clock, iteration length and forcing.
  *
  * Layout of a scenario in HBM: binary32 fields with a 4-cell halo
- * (rows + 8 rows of `pitch` floats, pitch a multiple of 32), cell (r, c) at
- * (r + 4) * pitch + (c + 4).  The bed is stored as binary32 offsets from a
- * per-tile datum (a multiple of 1/16 m, so datum differences are exact in
- * binary32); the info byte holds the active bit and the Manning class.
+ * ((rows + 8) rows of `pitch` floats, pitch >= cols + 12 and a multiple of
+ * 32), cell (r, c) at (r + 4) * pitch + (c + 4).  The bed is stored as
+ * binary32 offsets from the datum of the cell's (strip, segment) tile, a
+ * multiple of 1/16 m so datum differences are exact in binary32; inactive
+ * cells (NODATA and the halo) hold NaN as bed offset.  Manning classes, when
+ * present, are one byte per cell.
  */
 #ifndef SW2D_FP32_H
 #define SW2D_FP32_H
@@ -20,20 +22,18 @@
 
 namespace sw2d {
 
-constexpr int T32_TC = 64;  /* tile columns */
-constexpr int T32_TR = 32;  /* tile rows */
-constexpr int T32_H = 4;    /* halo */
-constexpr int T32_LW = T32_TC + 2 * T32_H; /* 72: staged tile width (floats) */
-constexpr int T32_LH = T32_TR + 2 * T32_H; /* 40: staged tile height */
-constexpr int T32_LWB = 80; /* staged byte-tile width (TMA inner extent multiple of 16 B) */
-constexpr int T32_NT = 256; /* threads per tile */
+constexpr int M_H = 4;                 /* halo */
+constexpr int M_NW = 4;                /* warps per CTA */
+constexpr int M_SW = 56;               /* output columns per warp (2 per lane, lanes 2..29) */
+constexpr int M_CW = M_NW * M_SW;      /* 224 output columns per strip */
+constexpr int M_BW = M_CW + 2 * M_H;   /* 232 staged columns */
+constexpr int M_RB = 4;                /* rows per staged block (TMA box height) */
+constexpr int M_NS = 3;                /* blocks in the staging ring */
+constexpr int M_NT = M_NW * 32;
 constexpr int T32_MAXCLASS = 64;
-constexpr int T32_MAXSRC = 16;
-
-#define SW2D_I_ACTIVE 1u /* info bit 0; bits 1..6: Manning class */
 
 /* Length and forcing of a scenario's next iteration, written by the
- * finalize kernel, read by every tile of the scenario. */
+ * finalize kernel, read by every work item of the scenario. */
 struct Slot32 {
     float dt2, dt2dx, dt2dy;
     float rr1, rr2;     /* rain rate, m/s */
@@ -66,19 +66,20 @@ struct Part32 {
 };
 
 struct Scn32 {
-    CUtensorMap tm_h[2], tm_qx[2], tm_qy[2], tm_z, tm_info;
+    CUtensorMap tm_h[2], tm_qx[2], tm_qy[2], tm_z;
     float* h[2];
     float* qx[2];
     float* qy[2];
     float* kc;             /* Kahan compensation of the depth */
+    const float* z;        /* bed offset (NaN = inactive), the TMA-mapped array */
     const float* datum;    /* per tile, tiles_y * tiles_x */
-    const uint8_t* info;   /* per cell (padded), the TMA-mapped array */
+    const uint8_t* cls;    /* Manning class per cell (padded) or NULL */
     const float* rainw;    /* per cell (padded) or NULL */
     const double* rain;    /* nrain + 2, mm per dtrain */
     const double* evap;    /* nevap + 2 or NULL */
     double* outlet;        /* outlet ring (t, Q) or NULL */
     Clock32* clk;
-    int R, C, P, tiles_x, tiles_y;
+    int R, C, P, tiles_x, tiles_y, seg;
     int first_work, nwork;
     int outflow_south, ledger_cells, series_mode, dt_mode;
     int nrain, nevap, outlet_cap;
