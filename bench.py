@@ -192,6 +192,100 @@ def run_fp32_leg(args, peak):
     }
 
 
+def make_batch_specs(n, lo, hi, seed, t_scale=1.0):
+    """Scenarios of the batched form: square rasters with side log-uniform in
+    [lo, hi], fractal DEM (Hurst U(0.7, 0.9)) on a 1% tilt, 3-class Voronoi n,
+    gamma hyetograph (mean U(5, 60) mm/h, duration U(1, 6) h), dx = 1 m."""
+    from sw2d_efdc_gb300 import api, synth
+    rng = np.random.default_rng(seed)
+    sides = synth.loguniform_sides(n, lo, hi, rng)
+    specs = []
+    for side in sides:
+        sc = synth.batch_scenario(int(side), rng, dx=1.0)
+        specs.append(dict(dem=sc.dem, manning_classes=sc.manning_classes, manning_table=sc.manning_table,
+                          rain_mm=sc.rain_mm, dtrain=sc.dtrain, dx=1.0, t_end=sc.t_end * t_scale,
+                          outflow=api.OUTFLOW_SOUTH, cfl=sc.cfl, dt_max=sc.dt_max))
+    return specs
+
+
+def run_batched_leg(args, peak, fp64_value):
+    """configs[3]: 256 scenarios of uneven size advanced together, one fused
+    launch per iteration (graph-captured chunks), each with its own CFL length."""
+    from sw2d_efdc_gb300 import api
+    t0 = time.time()
+    specs = make_batch_specs(args.batch_n, 128, 2048, 4)
+    gen_s = time.time() - t0
+    b = api.Batch()
+    for sp in specs:
+        b.submit(**sp)
+    b.step(0)
+    b.step(max(args.warmup, 3))
+    st0 = b.stats()
+    b.step(args.steps)
+    st1 = b.stats()
+    cells = sum(sp["dem"].size for sp in specs)
+    ms = st1["device_ms"] - st0["device_ms"]
+    cu = st1["cell_updates"] - st0["cell_updates"]
+    b.close()
+    value = cu / (ms * 1e-3) / 1e9
+    achieved = value * BYTES_PER_CELL_FP32_CFG3 * 1e9 / 1e9
+    return {"value": round(value, 4), "unit": UNIT, "scenarios": len(specs), "cells": int(cells),
+            "steps": args.steps, "ms_per_step": round(ms / args.steps, 4),
+            "workload": "batched FP32: %d scenarios, side log-uniform 128-2048, fractal DEM, 3-class Voronoi n, "
+                        "gamma hyetographs, per-scenario CFL length, one fused launch per iteration" % len(specs),
+            "roofline": {"bound": "hbm", "kernel": "k32_march + k32_finalize", "achieved": round(achieved, 2),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3 + 1},
+            "vs_fp64_plain": round(value / fp64_value, 3) if fp64_value else None,
+            "input_generation_s": round(gen_s, 1)}
+
+
+def run_served_leg(args, fp64_value):
+    """configs[4]: a finite Poisson trace of requests (lambda 20/s, side
+    log-uniform 256-4096) admitted against an HBM budget as they arrive and
+    advanced step by step together; completion latency = finish - arrival."""
+    from sw2d_efdc_gb300 import api, synth
+    rng = np.random.default_rng(5)
+    n = args.serve_n
+    arrivals = synth.poisson_arrivals(n, 20.0, rng)
+    t0 = time.time()
+    specs = make_batch_specs(n, 256, 4096, 6, t_scale=args.serve_time_scale)
+    gen_s = time.time() - t0
+    b = api.Batch(hbm_budget_bytes=150e9)
+    ids = {}
+    done = {}
+    start = time.perf_counter()
+    nxt = 0
+    while len(done) < n:
+        now = time.perf_counter() - start
+        while nxt < n and arrivals[nxt] <= now:
+            ids[b.submit(**specs[nxt])] = nxt
+            nxt += 1
+        nr, nq = b.step(args.serve_chunk)
+        now = time.perf_counter() - start
+        for rid, k in list(ids.items()):
+            if k in done:
+                continue
+            st, _ = b.poll(rid)
+            if st == api.REQ_DONE:
+                done[k] = now
+        if nr == 0 and nq == 0 and nxt < n:
+            time.sleep(max(0.0, arrivals[nxt] - now))
+    wall = time.perf_counter() - start
+    stats = b.stats()
+    b.close()
+    lat = np.array([done[k] - arrivals[k] for k in range(n)])
+    return {"requests": n, "lambda_per_s": 20.0, "wall_s": round(wall, 2),
+            "latency_p50_s": round(float(np.percentile(lat, 50)), 3),
+            "latency_p99_s": round(float(np.percentile(lat, 99)), 3),
+            "value": round(stats["cell_updates"] / (stats["device_ms"] * 1e-3) / 1e9, 4), "unit": UNIT,
+            "vs_fp64_plain": round(stats["cell_updates"] / (stats["device_ms"] * 1e-3) / 1e9 / fp64_value, 3)
+            if fp64_value else None,
+            "workload": "served FP32: Poisson arrivals 20/s, side log-uniform 256-4096, durations U(1,6) h x %g, "
+                        "HBM budget 150 GB, continuous admission" % args.serve_time_scale,
+            "input_generation_s": round(gen_s, 1)}
+
+
 def run_ours(args):
     rank, local, world = dist_env()
     from sw2d_efdc_gb300 import api
@@ -292,6 +386,10 @@ def run_ours(args):
     if not args.no_fp32:
         out["fp32_precision_form"] = run_fp32_leg(args, peak)
         out["fp32_precision_form"]["vs_fp64_plain"] = round(out["fp32_precision_form"]["value"] / value, 3)
+    if args.batch_n > 0:
+        out["fp32_batched"] = run_batched_leg(args, peak, value)
+    if args.serve_n > 0:
+        out["served"] = run_served_leg(args, value)
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, secs, n = cpu_reference_sample(sc, args.cpu_iters, 1, threads, h0=h_spun)
@@ -341,6 +439,11 @@ def main():
     ap.add_argument("--fp32-size", type=int, default=8192)
     ap.add_argument("--fp32-spinup-s", type=float, default=300.0)
     ap.add_argument("--fp64-only", action="store_true")
+    ap.add_argument("--batch-n", type=int, default=256, help="scenarios of the batched leg (0 = skip)")
+    ap.add_argument("--serve-n", type=int, default=48, help="requests of the served leg (0 = skip)")
+    ap.add_argument("--serve-time-scale", type=float, default=0.05,
+                    help="fraction of each request's 1-6 h duration simulated (bounded bench time)")
+    ap.add_argument("--serve-chunk", type=int, default=32)
     ap.add_argument("--spinup-s", type=float, default=60.0, help="simulated seconds before timing")
     ap.add_argument("--spinup-iters", type=int, default=0, help="iterations before timing (overrides --spinup-s)")
     args = ap.parse_args()
