@@ -156,7 +156,7 @@ def cpu_reference_sample(sc, iters: int, warm: int, threads: int, h0=None):
 
 def run_fp32_leg(args, peak):
     """FP32 precision form on the 8192 x 8192 dx = 1 m tilted-plane raster with a
-    gamma hyetograph (the fused TMA tile kernel), spun up, then K iterations."""
+    gamma hyetograph (the row-marching TMA kernel), spun up, then K iterations."""
     from sw2d_efdc_gb300 import api, synth
     size = args.fp32_size
     sc = synth.config3(rows=size, cols=size)
@@ -183,7 +183,7 @@ def run_fp32_leg(args, peak):
         "workload": "FP32 precision form %dx%d dx=1m tilted plane + bumps, gamma 5-min hyetograph "
                     "(shape 0.8, mean 20 mm/h), CFL 0.7, free south outlet, timed from t=%.0f s"
                     % (sc.rows, sc.cols, t_spun),
-        "roofline": {"bound": "hbm", "kernel": "k32_step (fused TMA tile) + k32_finalize",
+        "roofline": {"bound": "hbm", "kernel": "k32_march + k32_finalize",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3,
                      "traffic": None},

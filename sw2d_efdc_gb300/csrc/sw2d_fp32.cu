@@ -89,15 +89,11 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
 
 /* ---------------- device helpers ---------------------------------------- */
 
-__device__ __forceinline__ float rpow_manning_f32(float hm) {
-    /* hm^-1.3333330 from the hardware log2/exp2 (relative error ~1e-6) */
-    return __powf(hm, -1.3333330f);
-}
-
-/* binary32 square root and quotient from the hardware reciprocal
- * approximations (a few ulp; the precision form does not need IEEE rounding) */
+/* binary32 math from the hardware approximations (a few ulp; the precision
+ * form does not need IEEE rounding) */
+__device__ __forceinline__ float frcp(float x) { return __frcp_rn(x); }
 __device__ __forceinline__ float fsqrt(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
-__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float rpow_manning_f32(float hm) { return __powf(hm, -1.3333330f); } /* hm^-1.333333 */
 
 __device__ __forceinline__ bool is_act(float z) { return z == z; } /* NaN bed offset = inactive */
 
@@ -105,7 +101,7 @@ __device__ __forceinline__ bool is_act(float z) { return z == z; } /* NaN bed of
  * columns (2l, 2l+1) */
 __device__ __forceinline__ float2 left2(float2 v) { return make_float2(__shfl_up_sync(0xffffffffu, v.y, 1), v.x); }
 __device__ __forceinline__ float2 right2(float2 v) { return make_float2(v.y, __shfl_down_sync(0xffffffffu, v.x, 1)); }
-__device__ __forceinline__ int leftbits(int v) { /* bit k = column k; returns neighbours' bits */
+__device__ __forceinline__ int leftbits(int v) { /* bit k = column k; returns the left neighbours' bits */
     const int up = __shfl_up_sync(0xffffffffu, v, 1);
     return ((up >> 1) & 1) | ((v & 1) << 1);
 }
@@ -119,62 +115,50 @@ __device__ __forceinline__ void setc(float2& v, int k, float x) {
     else v.x = x;
 }
 
-struct FluxIn {
-    float hw, he, zw, ze;          /* cells either side (w = north / s = west) */
-    float nw, ne;                  /* Manning n of the two cells */
-    float u0, uA, uB;              /* velocity on the face, and on the faces before / after along the normal */
-    float q0, qA, qB, qL, qR;      /* old discharge on the face, along the normal, across */
-    float v0, v1, v2, v3;          /* the four cross velocities of the friction and cross convection */
-    bool cross;                    /* cross-convection term present (not column 0 / row 0) */
+/* Upwind donor-cell transport across the edge between two faces of the same
+ * orientation (the reference's umr/uml, umu/umd, vnr/vnl, vnu/vnd terms,
+ * SW2D-EFDC.cu:171-189, :288-306): with a = half the mean of the two face
+ * velocities, a (q1 + q0) + |a| (q0 - q1), q0 on the upstream-indexed face.
+ * Each edge is shared by the two faces it separates, so it is computed once. */
+__device__ __forceinline__ float edge_term(float w_quarter, float q0, float q1) {
+    return w_quarter * (q1 + q0) + fabsf(w_quarter) * (q0 - q1);
+}
+
+struct FaceIn {
+    float hw, he, zw, ze;  /* the two cells (w: north / west, e: south / east) */
+    float q0, u0, vt;      /* old discharge, face velocity, cross velocity at the face */
+    float along, across;   /* convection differences (edge terms, already scaled) */
+    float gdt2n;           /* g * dt2 / spacing along the normal */
+    float gn2;             /* g * n_face^2 */
 };
 
-/* One face of the reference's flux (SW2D-EFDC.cu:110-202 for x, :228-319
- * for y), in binary32.  For x faces: A = north face, B = south face,
- * L/R = west/east faces, v0..v3 = vv1 at (r,c), (r,c+1), (r-1,c), (r-1,c+1).
- * For y faces: A = west face, B = east face, L/R = north/south faces along
- * x (v11 term), v0..v3 = uu1 at (r,c), (r+1,c), (r,c-1), (r+1,c-1). */
-__device__ __forceinline__ float face_flux(const FluxIn& f, float th, float gg, float dt2, float dt2n, float dt2t,
-                                           bool is_x) {
+/* One face of the reference's flux (SW2D-EFDC.cu:110-202 x, :228-319 y) in
+ * binary32, evaluated without branches so that a lane's four faces
+ * interleave: the weir / dry-bed / momentum results are selected by the
+ * reference's conditions. */
+__device__ __forceinline__ float face_flux(const FaceIn& f, float th, float g, float hdt2) {
     const float he = f.he, hw = f.hw, ze = f.ze, zw = f.zw;
-    if (!is_act(ze) || !is_act(zw)) return 0.f;
-    if (!((hw > th) || (he > th))) return 0.f;
+    const bool act = is_act(ze) && is_act(zw);
+    const bool wet = (hw > th) || (he > th);
     const float hhe = he + ze, hhw = hw + zw;
     const float hhep = he - th, hhwp = hw - th;
-    if (hhe < zw) return hw > th ? 0.5440f * hw * fsqrt(gg * hw) : 0.f;
-    if (hhw < ze) return he > th ? -0.544f * he * fsqrt(gg * he) : 0.f;
-    if (hhep * hhwp < 0.f) {
-        if ((he > 0.f) || (hw > 0.f)) {
-            const float sg = copysignf(1.f, hhep - hhwp);
-            const float hh3 = fmaxf(hhe, hhw) - fmaxf(ze, zw);
-            return -sg * 0.350f * hh3 * fsqrt(2.f * gg * hh3);
-        }
-        return 0.f;
-    }
+    const bool d1a = hhe < zw, d1b = hhw < ze;
+    const bool d2 = hhep * hhwp < 0.f;
+    /* dry bed 1: free overfall from the higher cell (:129-144) */
+    const float hup = d1a ? hw : he;
+    const float fw = (hup > th) ? (d1a ? 0.5440f : -0.544f) * hup * fsqrt(g * hup) : 0.f;
+    /* dry bed 2 (:148-157) */
+    const float hh3 = fmaxf(hhe, hhw) - fmaxf(ze, zw);
+    const float fd = ((he > 0.f) || (hw > 0.f)) ? -copysignf(0.350f, hhep - hhwp) * hh3 * fsqrt(2.f * g * hh3) : 0.f;
+    /* momentum: gravity, convection, semi-implicit Manning friction (:165-202) */
     const float hm = 0.5f * (he + hw);
-    const float grav = gg * hm * dt2n * ((he - hw) + (ze - zw));
-    /* convection along the normal */
-    const float aB = 0.5f * (f.uB + f.u0), aA = 0.5f * (f.u0 + f.uA);
-    const float cB = aB * (f.qB + f.q0) * 0.5f + fabsf(aB) * (f.q0 - f.qB) * 0.5f;
-    const float cA = aA * (f.q0 + f.qA) * 0.5f + fabsf(aA) * (f.qA - f.q0) * 0.5f;
-    const float along = dt2n * (cB - cA);
-    /* convection across */
-    float across = 0.f;
-    if (f.cross) {
-        (void)is_x;
-        const float wu = 0.5f * (f.v1 + f.v3), wd = 0.5f * (f.v0 + f.v2);
-        const float cu = wu * (f.qR + f.q0) * 0.5f + fabsf(wu) * (f.q0 - f.qR) * 0.5f;
-        const float cd = wd * (f.qL + f.q0) * 0.5f + fabsf(wd) * (f.qL - f.q0) * 0.5f;
-        across = dt2t * (cu - cd);
-    }
-    const float vt = 0.25f * (f.v0 + f.v1 + f.v2 + f.v3);
-    const float sq = fsqrt(f.u0 * f.u0 + vt * vt);
-    float ram = 0.f;
-    if (hm > th) {
-        const float nf = 0.5f * (f.ne + f.nw);
-        ram = gg * nf * nf * sq * rpow_manning_f32(hm);
-    }
-    const float a = dt2 * ram * 0.5f;
-    return fdiv((1.f - a) * f.q0 + (-along - across - grav), 1.f + a);
+    const float grav = f.gdt2n * hm * ((he - hw) + (ze - zw));
+    const float sq = fsqrt(f.u0 * f.u0 + f.vt * f.vt);
+    const float ram = (hm > th) ? f.gn2 * sq * rpow_manning_f32(hm) : 0.f;
+    const float a = hdt2 * ram;
+    const float fm = ((1.f - a) * f.q0 - f.along - f.across - grav) * frcp(1.f + a);
+    const float F = (d1a || d1b) ? fw : (d2 ? fd : fm);
+    return (act && wet) ? F : 0.f;
 }
 
 /* ---------------- the row-marching step ---------------------------------- */
@@ -244,18 +228,20 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
     const float dzt0 = S.dd[creg0], dzm0 = S.dd[3 + creg0], dzb0 = S.dd[6 + creg0];
     const float dzt1 = S.dd[creg1], dzm1 = S.dd[3 + creg1], dzb1 = S.dd[6 + creg1];
     const float th = P.th, gg = P.g, rdx = P.rdx, rdy = P.rdy;
-    const float dt2 = sl.dt2, dt2dx = sl.dt2dx, dt2dy = sl.dt2dy;
+    const float dt2 = sl.dt2, dt2dx = sl.dt2dx, dt2dy = sl.dt2dy, hdt2 = 0.5f * sl.dt2;
+    const float gdx = gg * dt2dx, gdy = gg * dt2dy;
     const bool has_cls = P.cls != nullptr, has_rw = P.rainw != nullptr;
-    const float n_uni = S.ntab[0];
+    const float n_uni = S.ntab[0], gn2_uni = gg * n_uni * n_uni;
+    const bool col0_0 = (cg == 0), col0_1 = (cg + 1 == 0);
 
-    /* register windows, slot = row & 3 relative to Ls */
+    /* register windows, slot = (row - Ls) & 3 */
     float2 H[4], Z[4], QX[4], QY[4], U[4], V[4], FX[4], FY[4];
-    float2 HL[4], ZL[4], UL[4], VR[4], FYR[4], RW[4], NN[4], NL[4];
+    float2 HL[4], ZL[4], UL[4], VR[4], FYR[4], RW[4], NN[4], NL[4], EX[4], GY[4];
     int DRY[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         H[k] = Z[k] = QX[k] = QY[k] = U[k] = V[k] = FX[k] = FY[k] = make_float2(0.f, 0.f);
-        HL[k] = ZL[k] = UL[k] = VR[k] = FYR[k] = NN[k] = NL[k] = make_float2(0.f, 0.f);
+        HL[k] = ZL[k] = UL[k] = VR[k] = FYR[k] = NN[k] = NL[k] = EX[k] = GY[k] = make_float2(0.f, 0.f);
         RW[k] = make_float2(1.f, 1.f);
         DRY[k] = 0;
     }
@@ -288,7 +274,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         for (int j = 0; j < RB; j++) {
             const int L = Ls + b * RB + j;
             const int s0 = j & 3, s1 = (j + 3) & 3, s2 = (j + 2) & 3, s3 = (j + 1) & 3; /* L, L-1, L-2, L-3 */
-            /* ---- load row L ---- */
+            /* ---- row L from the staged block ---- */
             H[s0] = *reinterpret_cast<const float2*>(sh + j * BW + sc);
             float2 zz = *reinterpret_cast<const float2*>(sz + j * BW + sc);
             zz.x += L < rs ? dzt0 : (L >= re ? dzb0 : dzm0);
@@ -296,110 +282,97 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
             Z[s0] = zz;
             QX[s0] = *reinterpret_cast<const float2*>(sqx + j * BW + sc);
             QY[s0] = *reinterpret_cast<const float2*>(sqy + j * BW + sc);
+            const bool rowin = (L >= -M_H && L < R + M_H) && cg + M_H >= 0 && cg + M_H + 1 < Pp;
+            const size_t gL = (size_t)(L + M_H) * Pp + (cg + M_H);
             if (has_cls) {
-                const size_t g = (size_t)(L + M_H) * Pp + (cg + M_H);
-                float2 nn;
-                if (L >= -M_H && L < R + M_H && cg + M_H >= 0 && cg + M_H + 1 < Pp) {
-                    const uchar2 cc = *reinterpret_cast<const uchar2*>(P.cls + g);
+                float2 nn = make_float2(n_uni, n_uni);
+                if (rowin) {
+                    const uchar2 cc = *reinterpret_cast<const uchar2*>(P.cls + gL);
                     nn = make_float2(S.ntab[cc.x & 63], S.ntab[cc.y & 63]);
-                } else {
-                    nn = make_float2(n_uni, n_uni);
                 }
                 NN[s0] = nn;
                 NL[s0] = left2(nn);
-            } else {
-                NN[s0] = NL[s0] = make_float2(n_uni, n_uni);
             }
-            if (has_rw) {
-                const size_t g = (size_t)(L + M_H) * Pp + (cg + M_H);
-                RW[s0] = (L >= -M_H && L < R + M_H && cg + M_H >= 0 && cg + M_H + 1 < Pp)
-                             ? *reinterpret_cast<const float2*>(P.rainw + g)
-                             : make_float2(1.f, 1.f);
-            }
-            /* ---- face velocities of row L; CFL face speeds of owned faces ---- */
+            if (has_rw) RW[s0] = rowin ? *reinterpret_cast<const float2*>(P.rainw + gL) : make_float2(1.f, 1.f);
             HL[s0] = left2(H[s0]);
             ZL[s0] = left2(Z[s0]);
+            /* ---- face velocities of row L and CFL face speeds of owned faces ---- */
             const bool rowown = (L >= rs && L < re);
 #pragma unroll
             for (int k = 0; k < 2; k++) {
-                const float hLk = comp(H[s0], k), hUk = comp(H[s1], k);
-                const float hm = (L == R) ? hUk : 0.5f * (hLk + hUk);
-                const float q = comp(QX[s0], k);
-                const float u = (hm >= th && q != 0.f) ? fdiv(q, hm) : 0.f;
+                const float hLk = comp(H[s0], k);
+                const float hm = (L == R) ? comp(H[s1], k) : 0.5f * (hLk + comp(H[s1], k));
+                const float u = (hm >= th) ? comp(QX[s0], k) * frcp(hm) : 0.f;
                 setc(U[s0], k, u);
                 const float hn = 0.5f * (hLk + comp(HL[s0], k));
-                const float qy = comp(QY[s0], k);
-                const float v = (hn >= th && qy != 0.f) ? fdiv(qy, hn) : 0.f;
+                const float v = (hn >= th) ? comp(QY[s0], k) * frcp(hn) : 0.f;
                 setc(V[s0], k, v);
-                const bool own = k ? own1 : own0;
-                if (rowown && own) {
-                    if (hm >= th && is_act(comp(Z[s0], k)) && is_act(comp(Z[s1], k)))
-                        sxm = fmaxf(sxm, (fabsf(u) + fsqrt(gg * hm)) * rdx);
-                    if (hn >= th && is_act(comp(Z[s0], k)) && is_act(comp(ZL[s0], k)))
-                        sym = fmaxf(sym, (fabsf(v) + fsqrt(gg * hn)) * rdy);
-                }
+                const bool own = (k ? own1 : own0) && rowown;
+                const bool za = is_act(comp(Z[s0], k));
+                const bool okx = own && hm >= th && za && is_act(comp(Z[s1], k));
+                const bool oky = own && hn >= th && za && is_act(comp(ZL[s0], k));
+                sxm = fmaxf(sxm, okx ? (fabsf(u) + fsqrt(gg * hm)) * rdx : 0.f);
+                sym = fmaxf(sym, oky ? (fabsf(v) + fsqrt(gg * hn)) * rdy : 0.f);
             }
             UL[s0] = left2(U[s0]);
             VR[s0] = right2(V[s0]);
-            /* ---- face discharges of row L-1 ---- */
-            {
-                const float2 qxl = left2(QX[s1]), qxr = right2(QX[s1]);
-                const float2 qyl = left2(QY[s1]), qyr = right2(QY[s1]);
-                const float2 vl = left2(V[s1]);
-                const int rf = L - 1;
+            /* ---- edge terms: along x between x faces L-1 and L, cross for y faces
+             *      between rows L-1 and L, and the two edge kinds of row L-1 ---- */
+            const float2 qxr = right2(QX[s1]), qyr = right2(QY[s1]);
+            float2 EY, GX;
 #pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const int c = cg + k;
-                    FluxIn fx;
-                    fx.hw = comp(H[s2], k);
-                    fx.he = comp(H[s1], k);
-                    fx.zw = comp(Z[s2], k);
-                    fx.ze = comp(Z[s1], k);
-                    fx.nw = comp(NN[s2], k);
-                    fx.ne = comp(NN[s1], k);
-                    fx.u0 = comp(U[s1], k);
-                    fx.uA = comp(U[s2], k);
-                    fx.uB = comp(U[s0], k);
-                    fx.q0 = comp(QX[s1], k);
-                    fx.qA = comp(QX[s2], k);
-                    fx.qB = comp(QX[s0], k);
-                    fx.qL = comp(qxl, k);
-                    fx.qR = comp(qxr, k);
-                    fx.v0 = comp(V[s1], k);
-                    fx.v1 = comp(VR[s1], k);
-                    fx.v2 = comp(V[s2], k);
-                    fx.v3 = comp(VR[s2], k);
-                    fx.cross = (c != 0);
-                    float F;
-                    if (rf == R && P.outflow_south) {
-                        const float hwk = fx.hw;
-                        F = (is_act(fx.zw) && hwk > th) ? 0.5440f * hwk * fsqrt(gg * hwk) : 0.f;
-                    } else {
-                        F = face_flux(fx, th, gg, dt2, dt2dx, dt2dy, true);
-                    }
-                    setc(FX[s1], k, F);
-                    FluxIn fy;
-                    fy.hw = comp(HL[s1], k);
-                    fy.he = comp(H[s1], k);
-                    fy.zw = comp(ZL[s1], k);
-                    fy.ze = comp(Z[s1], k);
-                    fy.nw = comp(NL[s1], k);
-                    fy.ne = comp(NN[s1], k);
-                    fy.u0 = comp(V[s1], k);
-                    fy.uA = comp(vl, k);
-                    fy.uB = comp(VR[s1], k);
-                    fy.q0 = comp(QY[s1], k);
-                    fy.qA = comp(qyl, k);
-                    fy.qB = comp(qyr, k);
-                    fy.qL = comp(QY[s2], k);
-                    fy.qR = comp(QY[s0], k);
-                    fy.v0 = comp(U[s1], k);
-                    fy.v1 = comp(U[s0], k);
-                    fy.v2 = comp(UL[s1], k);
-                    fy.v3 = comp(UL[s0], k);
-                    fy.cross = (rf != 0);
-                    setc(FY[s1], k, face_flux(fy, th, gg, dt2, dt2dy, dt2dx, false));
+            for (int k = 0; k < 2; k++) {
+                setc(EX[s1], k, edge_term(0.25f * (comp(U[s0], k) + comp(U[s1], k)), comp(QX[s1], k), comp(QX[s0], k)));
+                setc(GY[s1], k, edge_term(0.25f * (comp(U[s0], k) + comp(UL[s0], k)), comp(QY[s1], k), comp(QY[s0], k)));
+                setc(EY, k, edge_term(0.25f * (comp(VR[s1], k) + comp(V[s1], k)), comp(QY[s1], k), comp(qyr, k)));
+                setc(GX, k, edge_term(0.25f * (comp(VR[s1], k) + comp(VR[s2], k)), comp(QX[s1], k), comp(qxr, k)));
+            }
+            const float2 EYL = left2(EY), GXL = left2(GX);
+            /* ---- face discharges of row L-1 ---- */
+            const int rf = L - 1;
+#pragma unroll
+            for (int k = 0; k < 2; k++) {
+                FaceIn fx;
+                fx.hw = comp(H[s2], k);
+                fx.he = comp(H[s1], k);
+                fx.zw = comp(Z[s2], k);
+                fx.ze = comp(Z[s1], k);
+                fx.q0 = comp(QX[s1], k);
+                fx.u0 = comp(U[s1], k);
+                fx.vt = 0.25f * (comp(V[s1], k) + comp(V[s2], k) + comp(VR[s1], k) + comp(VR[s2], k));
+                fx.along = dt2dx * (comp(EX[s1], k) - comp(EX[s2], k));
+                fx.across = (k ? col0_1 : col0_0) ? 0.f : dt2dy * (comp(GX, k) - comp(GXL, k));
+                fx.gdt2n = gdx;
+                if (has_cls) {
+                    const float nf = 0.5f * (comp(NN[s1], k) + comp(NN[s2], k));
+                    fx.gn2 = gg * nf * nf;
+                } else {
+                    fx.gn2 = gn2_uni;
                 }
+                float F = face_flux(fx, th, gg, hdt2);
+                if (rf == R) { /* south edge: free overfall when open (SW2D-EFDC.cu:131 law) */
+                    const float hw = fx.hw;
+                    F = (P.outflow_south && is_act(fx.zw) && hw > th) ? 0.5440f * hw * fsqrt(gg * hw) : 0.f;
+                }
+                setc(FX[s1], k, F);
+                FaceIn fy;
+                fy.hw = comp(HL[s1], k);
+                fy.he = comp(H[s1], k);
+                fy.zw = comp(ZL[s1], k);
+                fy.ze = comp(Z[s1], k);
+                fy.q0 = comp(QY[s1], k);
+                fy.u0 = comp(V[s1], k);
+                fy.vt = 0.25f * (comp(U[s1], k) + comp(U[s0], k) + comp(UL[s1], k) + comp(UL[s0], k));
+                fy.along = dt2dy * (comp(EY, k) - comp(EYL, k));
+                fy.across = (rf == 0) ? 0.f : dt2dx * (comp(GY[s1], k) - comp(GY[s2], k));
+                fy.gdt2n = gdy;
+                if (has_cls) {
+                    const float nf = 0.5f * (comp(NN[s1], k) + comp(NL[s1], k));
+                    fy.gn2 = gg * nf * nf;
+                } else {
+                    fy.gn2 = gn2_uni;
+                }
+                setc(FY[s1], k, face_flux(fy, th, gg, hdt2));
             }
             /* ---- provisional depth of row L-2 -> dry flags ---- */
             FYR[s2] = right2(FY[s2]);
@@ -408,14 +381,13 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
 #pragma unroll
                 for (int k = 0; k < 2; k++) {
                     const float ho = comp(H[s2], k);
-                    if (is_act(comp(Z[s2], k))) {
-                        const float pct = ho > P.ev_wl_min ? P.pct_lake : P.pct_land;
-                        const float ev = ho > P.ev_wl_min ? sl.ev1 : 0.f;
-                        const float hs = ho - dt2 * ((comp(FX[s1], k) - comp(FX[s2], k)) * rdx +
-                                                     (comp(FYR[s2], k) - comp(FY[s2], k)) * rdy -
-                                                     sl.rr1 * comp(RW[s2], k) * pct + ev);
-                        dry |= (hs < th) ? (1 << k) : 0;
-                    }
+                    const bool lake = ho > P.ev_wl_min;
+                    const float pct = lake ? P.pct_lake : P.pct_land;
+                    const float ev = lake ? sl.ev1 : 0.f;
+                    const float hs = ho - dt2 * ((comp(FX[s1], k) - comp(FX[s2], k)) * rdx +
+                                                 (comp(FYR[s2], k) - comp(FY[s2], k)) * rdy -
+                                                 sl.rr1 * comp(RW[s2], k) * pct + ev);
+                    dry |= (is_act(comp(Z[s2], k)) && hs < th) ? (1 << k) : 0;
                 }
                 DRY[s2] = dry;
             }
@@ -424,48 +396,46 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 const int r = L - 3;
                 const int dc = DRY[s3], dN = DRY[s0], dS = DRY[s2];
                 const int dW = leftbits(dc), dE = rightbits(dc);
-                if (r >= rs && r < re) {
+                if (r >= rs && r < re && (own0 || own1)) {
                     const size_t g = (size_t)(r + M_H) * Pp + (cg + M_H);
-                    float2 kcv = make_float2(0.f, 0.f);
-                    if (own0 || own1) kcv = own1 ? *reinterpret_cast<const float2*>(P.kc + g)
-                                                 : make_float2(P.kc[g], 0.f);
+                    const float2 kcv = own1 ? *reinterpret_cast<const float2*>(P.kc + g) : make_float2(P.kc[g], 0.f);
                     float2 hout, kout, fNo, fWo, fSo;
 #pragma unroll
                     for (int k = 0; k < 2; k++) {
                         float fN = comp(FX[s3], k), fS = comp(FX[s2], k), fW = comp(FY[s3], k), fE = comp(FYR[s3], k);
                         const int bc = (dc >> k) & 1;
-                        if ((fN > 0.f && ((dN >> k) & 1)) || (fN < 0.f && bc)) fN = 0.f;
-                        if ((fS > 0.f && bc) || (fS < 0.f && ((dS >> k) & 1))) fS = 0.f;
-                        if ((fW > 0.f && ((dW >> k) & 1)) || (fW < 0.f && bc)) fW = 0.f;
-                        if ((fE > 0.f && bc) || (fE < 0.f && ((dE >> k) & 1))) fE = 0.f;
-                        float hn = 0.f, kc = 0.f;
+                        fN = ((fN > 0.f && ((dN >> k) & 1)) || (fN < 0.f && bc)) ? 0.f : fN;
+                        fS = ((fS > 0.f && bc) || (fS < 0.f && ((dS >> k) & 1))) ? 0.f : fS;
+                        fW = ((fW > 0.f && ((dW >> k) & 1)) || (fW < 0.f && bc)) ? 0.f : fW;
+                        fE = ((fE > 0.f && bc) || (fE < 0.f && ((dE >> k) & 1))) ? 0.f : fE;
                         const bool own = k ? own1 : own0;
-                        if (is_act(comp(Z[s3], k))) {
-                            const float ho = comp(H[s3], k);
-                            const float wgt = comp(RW[s3], k);
-                            const float pct = ho > P.ev_wl_min ? P.pct_lake : P.pct_land;
-                            const float ev = ho > P.ev_wl_min ? sl.ev2 : 0.f;
-                            const float dh = -dt2 * ((fS - fN) * rdx + (fE - fW) * rdy - sl.rr2 * wgt * pct + ev);
-                            const float y = dh - comp(kcv, k);
-                            const float t = ho + y;
-                            kc = (t - ho) - y;
-                            hn = t;
-                            if (hn < 0.f) {
-                                if (own) clamp -= hn;
-                                hn = 0.f;
-                                kc = 0.f;
-                            }
-                            if (own && P.ledger_cells) {
+                        const bool act = is_act(comp(Z[s3], k));
+                        const float ho = comp(H[s3], k);
+                        const float wgt = comp(RW[s3], k);
+                        const bool lake = ho > P.ev_wl_min;
+                        const float pct = lake ? P.pct_lake : P.pct_land;
+                        const float ev = lake ? sl.ev2 : 0.f;
+                        const float dh = -dt2 * ((fS - fN) * rdx + (fE - fW) * rdy - sl.rr2 * wgt * pct + ev);
+                        /* Kahan: the increment is small against the depth */
+                        const float y = dh - comp(kcv, k);
+                        const float t = ho + y;
+                        float kc = (t - ho) - y;
+                        float hn = t;
+                        if (own && act) {
+                            clamp += hn < 0.f ? -hn : 0.f;
+                            if (P.ledger_cells) {
                                 rainacc += wgt * pct;
-                                evc += ho > P.ev_wl_min ? 1.f : 0.f;
+                                evc += lake ? 1.f : 0.f;
                             }
+                            if (r == R - 1) qout += fS;
                         }
+                        kc = (act && hn >= 0.f) ? kc : 0.f;
+                        hn = act ? fmaxf(hn, 0.f) : 0.f;
                         setc(hout, k, hn);
                         setc(kout, k, kc);
                         setc(fNo, k, fN);
                         setc(fWo, k, fW);
                         setc(fSo, k, fS);
-                        if (own && r == R - 1) qout += fS;
                     }
                     if (own0 && own1) {
                         *reinterpret_cast<float2*>(P.h[nxt] + g) = hout;
@@ -473,7 +443,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                         *reinterpret_cast<float2*>(P.qx[nxt] + g) = fNo;
                         *reinterpret_cast<float2*>(P.qy[nxt] + g) = fWo;
                         if (r == R - 1) *reinterpret_cast<float2*>(P.qx[nxt] + g + Pp) = fSo;
-                    } else if (own0) {
+                    } else {
                         P.h[nxt][g] = hout.x;
                         P.kc[g] = kout.x;
                         P.qx[nxt][g] = fNo.x;
