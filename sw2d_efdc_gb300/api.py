@@ -124,6 +124,9 @@ SIGNATURES = {
     "sw2d_batch_release": (C.c_int, [C.c_void_p, C.c_int64]),
     "sw2d_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
     "sw2d_batch_last_error": (C.c_char_p, []),
+    "sw2d_measure_state_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                             C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                             C.c_void_p, _dp, _dp]),
 }
 
 _lib = None
@@ -427,3 +430,16 @@ class Batch:
         st = BatchStats()
         _bcheck(load().sw2d_batch_get_stats(self._h, C.byref(st)), "sw2d_batch_get_stats")
         return {n: getattr(st, n) for n, _ in BatchStats._fields_}
+
+
+def measure_state_noalloc(dem_ptr, depth_ptr, qx_ptr, qy_ptr, rows, cols, dx, dy, nodata=-9999.0, th=1e-4,
+                          g=9.80, stream=0):
+    """Volume (m3) and CFL speed s of a state in caller-owned device memory
+    (raw device addresses of binary64 arrays in the sw2d_get_state layouts);
+    the call allocates no device memory.  Returns (volume, s)."""
+    vol = C.c_double()
+    spd = C.c_double()
+    _check(load().sw2d_measure_state_noalloc(dem_ptr, depth_ptr, qx_ptr, qy_ptr, int(rows), int(cols), float(dx),
+                                             float(dy), float(nodata), float(th), float(g), stream or None,
+                                             C.byref(vol), C.byref(spd)), "sw2d_measure_state_noalloc")
+    return vol.value, spd.value

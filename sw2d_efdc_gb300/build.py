@@ -31,6 +31,7 @@ UNITS = {
     "sw2d_engine.cu": [],
     "sw2d_batch.cu": [],
     "sw2d_api.cu": [],
+    "sw2d_noalloc.cu": ["--fmad=false", "-Xptxas", "-v"],
 }
 HEADERS = ["sw2d_internal.h", "sw2d_math.h", "sw2d_fp32.h", "sw2d_engine.h"]
 
@@ -50,7 +51,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 def _compile(unit: str) -> tuple[str, str]:
     src = os.path.join(CSRC, unit)
     obj = os.path.join(OBJ_DIR, unit.replace(".cu", ".o"))
-    deps = [src, os.path.join(ROOT, "include", "sw2d.h"), os.path.join(ROOT, "include", "sw2d_batch.h")] + \
+    deps = [src, os.path.join(ROOT, "include", "sw2d.h"), os.path.join(ROOT, "include", "sw2d_batch.h"),
+                  os.path.join(ROOT, "include", "sw2d_noalloc.h")] + \
         [os.path.join(CSRC, h) for h in HEADERS]
     if not _stale(obj, deps + [__file__]):
         return obj, ""

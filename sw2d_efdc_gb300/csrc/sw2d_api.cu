@@ -45,6 +45,11 @@ constexpr int kChunk = 32; /* iterations per captured graph (even) */
 
 } // namespace
 
+namespace sw2d {
+/* sets the message sw2d_last_error returns (for entry points in other units) */
+void set_error_message(const char* msg) { g_err = msg; }
+} // namespace sw2d
+
 struct sw2d_handle {
     sw2d_config cfg;
     int R = 0, C = 0, P = 0, NR = 0;
