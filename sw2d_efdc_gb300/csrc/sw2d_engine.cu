@@ -250,6 +250,9 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
         ok &= make_map(&d.tm_qy[k], d.qy[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, M_BW, M_RB, false);
     }
     ok &= make_map(&d.tm_z, dz, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, M_BW, M_RB, true);
+    ok &= make_map(&d.tm_kc, d.kc, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, M_BW, M_RB, false);
+    if (dcls) ok &= make_map(&d.tm_cls, dcls, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, P, NR, M_CLSW, M_CLSR, false);
+    if (drw) ok &= make_map(&d.tm_rw, drw, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, M_BW, M_RWR, false);
     if (!ok) {
         if (err) *err = "cuTensorMapEncodeTiled failed";
         return fail_free(SW2D_ERR_CUDA);

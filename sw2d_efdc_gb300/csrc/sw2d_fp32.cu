@@ -39,8 +39,19 @@ namespace sw2d {
 #define NS M_NS
 #define NT M_NT
 
+#define NF 5 /* staged fields: h, z, qx, qy, Kahan compensation (three rows behind) */
+
+struct alignas(128) ClsStage {
+    unsigned char v[M_CLSR][M_CLSW]; /* rows L-2 .. L+RB-1 of the block's first row L */
+};
+struct alignas(128) RwStage {
+    float v[M_RWR][BW]; /* rows L-3 .. L+RB-2 */
+};
+
 struct SmemM {
-    alignas(128) float stage[NS][4][RB][BW]; /* h, z, qx, qy */
+    alignas(128) float stage[NS][NF][RB][BW];
+    ClsStage cls[NS];
+    RwStage rw[NS];
     unsigned long long bar[NS];
     float ntab[T32_MAXCLASS];
     float dd[9];
@@ -48,6 +59,8 @@ struct SmemM {
     float redf[NW][2];
 };
 static_assert(offsetof(SmemM, stage) % 128 == 0, "TMA alignment");
+static_assert(offsetof(SmemM, cls) % 128 == 0 && sizeof(ClsStage) % 128 == 0, "TMA alignment");
+static_assert(offsetof(SmemM, rw) % 128 == 0 && sizeof(RwStage) % 128 == 0, "TMA alignment");
 static_assert((RB * BW * 4) % 128 == 0, "each staged array is whole 128-byte lines");
 static_assert((BW * 4) % 16 == 0, "TMA inner extent must be a multiple of 16 bytes");
 
@@ -89,16 +102,58 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
 
 /* ---------------- device helpers ---------------------------------------- */
 
-/* binary32 math from the hardware approximations (a few ulp; the precision
- * form does not need IEEE rounding) */
-__device__ __forceinline__ float frcp(float x) { return __frcp_rn(x); }
-__device__ __forceinline__ float fsqrt(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
-__device__ __forceinline__ float rpow_manning_f32(float hm) { return __powf(hm, -1.3333330f); } /* hm^-1.333333 */
+/* binary32 arithmetic from the hardware approximations (relative error a
+ * few 2^-23; the precision form does not need IEEE rounding) */
+__device__ __forceinline__ float rcpa(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrta(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float lg2a(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float ex2a(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float fsqrt(float x) { return sqrta(fmaxf(x, 0.f)); }
 
 __device__ __forceinline__ bool is_act(float z) { return z == z; } /* NaN bed offset = inactive */
 
-/* value of the neighbouring column on the left / right for the lane's two
- * columns (2l, 2l+1) */
+/* The lane's two columns (2l, 2l+1) travel as one float2 and most arithmetic
+ * is done on the pair with the packed FADD2 / FMUL2 / FFMA2 instructions. */
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); } /* a - b, one rounding */
+__device__ __forceinline__ float2 abs2(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(rcpa(a.x), rcpa(a.y)); }
+__device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrta(a.x), sqrta(a.y)); }
+/* m: bit 0 selects a.x, bit 1 selects a.y; else b */
+__device__ __forceinline__ float2 sel2(int m, float2 a, float2 b) {
+    return make_float2((m & 1) ? a.x : b.x, (m & 2) ? a.y : b.y);
+}
+__device__ __forceinline__ int ge2(float2 a, float t) { return (a.x >= t ? 1 : 0) | (a.y >= t ? 2 : 0); }
+__device__ __forceinline__ int gt2(float2 a, float t) { return (a.x > t ? 1 : 0) | (a.y > t ? 2 : 0); }
+__device__ __forceinline__ int lt2(float2 a, float t) { return (a.x < t ? 1 : 0) | (a.y < t ? 2 : 0); }
+__device__ __forceinline__ int act2(float2 z) { return (is_act(z.x) ? 1 : 0) | (is_act(z.y) ? 2 : 0); }
+
+/* hm^-1.3333330 = 2^(-1.3333330 log2 hm), the friction power (SW2D-EFDC.cu:193) */
+__device__ __forceinline__ float2 rpow_manning2(float2 hm) {
+    const float2 e = mul2(make_float2(lg2a(hm.x), lg2a(hm.y)), f2(-1.3333330f));
+    return make_float2(ex2a(e.x), ex2a(e.y));
+}
+
+/* value of the neighbouring column on the left / right */
 __device__ __forceinline__ float2 left2(float2 v) { return make_float2(__shfl_up_sync(0xffffffffu, v.y, 1), v.x); }
 __device__ __forceinline__ float2 right2(float2 v) { return make_float2(v.y, __shfl_down_sync(0xffffffffu, v.x, 1)); }
 __device__ __forceinline__ int leftbits(int v) { /* bit k = column k; returns the left neighbours' bits */
@@ -109,56 +164,65 @@ __device__ __forceinline__ int rightbits(int v) {
     const int dn = __shfl_down_sync(0xffffffffu, v, 1);
     return ((v >> 1) & 1) | ((dn & 1) << 1);
 }
-__device__ __forceinline__ float comp(float2 v, int k) { return k ? v.y : v.x; }
-__device__ __forceinline__ void setc(float2& v, int k, float x) {
-    if (k) v.y = x;
-    else v.x = x;
-}
 
 /* Upwind donor-cell transport across the edge between two faces of the same
  * orientation (the reference's umr/uml, umu/umd, vnr/vnl, vnu/vnd terms,
- * SW2D-EFDC.cu:171-189, :288-306): with a = half the mean of the two face
- * velocities, a (q1 + q0) + |a| (q0 - q1), q0 on the upstream-indexed face.
+ * SW2D-EFDC.cu:171-189, :288-306): with w = half the mean of the two face
+ * velocities, w (q1 + q0) + |w| (q0 - q1), q0 on the upstream-indexed face.
  * Each edge is shared by the two faces it separates, so it is computed once. */
-__device__ __forceinline__ float edge_term(float w_quarter, float q0, float q1) {
-    return w_quarter * (q1 + q0) + fabsf(w_quarter) * (q0 - q1);
+__device__ __forceinline__ float2 edge2(float2 w, float2 q0, float2 q1) {
+    return fma2(w, add2(q1, q0), mul2(abs2(w), sub2(q0, q1)));
 }
 
-struct FaceIn {
-    float hw, he, zw, ze;  /* the two cells (w: north / west, e: south / east) */
-    float q0, u0, vt;      /* old discharge, face velocity, cross velocity at the face */
-    float along, across;   /* convection differences (edge terms, already scaled) */
-    float gdt2n;           /* g * dt2 / spacing along the normal */
-    float gn2;             /* g * n_face^2 */
-};
-
-/* One face of the reference's flux (SW2D-EFDC.cu:110-202 x, :228-319 y) in
- * binary32, evaluated without branches so that a lane's four faces
- * interleave: the weir / dry-bed / momentum results are selected by the
- * reference's conditions. */
-__device__ __forceinline__ float face_flux(const FaceIn& f, float th, float g, float hdt2) {
-    const float he = f.he, hw = f.hw, ze = f.ze, zw = f.zw;
-    const bool act = is_act(ze) && is_act(zw);
-    const bool wet = (hw > th) || (he > th);
+/* Weir and dry-bed discharges of one face (SW2D-EFDC.cu:125-157), for the
+ * faces where the water surface on one side is below the other side's bed
+ * or exactly one side is wet. */
+__device__ __forceinline__ float face_special(float hw, float he, float zw, float ze, float th, float g) {
     const float hhe = he + ze, hhw = hw + zw;
-    const float hhep = he - th, hhwp = hw - th;
     const bool d1a = hhe < zw, d1b = hhw < ze;
-    const bool d2 = hhep * hhwp < 0.f;
-    /* dry bed 1: free overfall from the higher cell (:129-144) */
     const float hup = d1a ? hw : he;
     const float fw = (hup > th) ? (d1a ? 0.5440f : -0.544f) * hup * fsqrt(g * hup) : 0.f;
-    /* dry bed 2 (:148-157) */
     const float hh3 = fmaxf(hhe, hhw) - fmaxf(ze, zw);
-    const float fd = ((he > 0.f) || (hw > 0.f)) ? -copysignf(0.350f, hhep - hhwp) * hh3 * fsqrt(2.f * g * hh3) : 0.f;
-    /* momentum: gravity, convection, semi-implicit Manning friction (:165-202) */
-    const float hm = 0.5f * (he + hw);
-    const float grav = f.gdt2n * hm * ((he - hw) + (ze - zw));
-    const float sq = fsqrt(f.u0 * f.u0 + f.vt * f.vt);
-    const float ram = (hm > th) ? f.gn2 * sq * rpow_manning_f32(hm) : 0.f;
-    const float a = hdt2 * ram;
-    const float fm = ((1.f - a) * f.q0 - f.along - f.across - grav) * frcp(1.f + a);
-    const float F = (d1a || d1b) ? fw : (d2 ? fd : fm);
-    return (act && wet) ? F : 0.f;
+    const float fd =
+        ((he > 0.f) || (hw > 0.f)) ? -copysignf(0.350f, (he - th) - (hw - th)) * hh3 * fsqrt(2.f * g * hh3) : 0.f;
+    return (d1a || d1b) ? fw : fd;
+}
+
+struct Face2 {
+    float2 hw, he, zw, ze; /* the two cells (w: north / west, e: south / east) */
+    float2 q0, u0, vt;     /* old discharge, face velocity, cross velocity at the face */
+    float2 conv;           /* along + across convection, already scaled */
+    float2 fr;             /* -dt2/2 * g * n_face^2 */
+    int act;               /* both cells active, per column */
+};
+
+/* One face pair of the reference's flux (SW2D-EFDC.cu:110-202 x, :228-319 y)
+ * in binary32.  The momentum update (gravity, convection, semi-implicit
+ * Manning friction) is evaluated for both columns; the weir / dry-bed forms
+ * only when some lane of the warp needs them. */
+__device__ __forceinline__ float2 face_flux2(const Face2& f, float th, float g, float gdt2n) {
+    const float2 hm = mul2(add2(f.he, f.hw), f2(0.5f));
+    const float2 grav = mul2(mul2(f2(gdt2n), hm), add2(sub2(f.he, f.hw), sub2(f.ze, f.zw)));
+    const float2 sq = sqrt2(fma2(f.u0, f.u0, mul2(f.vt, f.vt)));
+    float2 an = mul2(mul2(f.fr, sq), rpow_manning2(hm)); /* -dt2/2 * friction */
+    an = sel2(gt2(hm, th), an, f2(0.f));
+    const float2 num = sub2(fma2(an, f.q0, f.q0), add2(f.conv, grav));
+    const float2 fm = mul2(num, rcp2(sub2(f2(1.f), an)));
+    /* which form applies (SW2D-EFDC.cu:115-165) */
+    const int wet = gt2(f.hw, th) | gt2(f.he, th);
+    const float2 hhe = add2(f.he, f.ze), hhw = add2(f.hw, f.zw);
+    const int d1a = ((hhe.x < f.zw.x) ? 1 : 0) | ((hhe.y < f.zw.y) ? 2 : 0);
+    const int d1b = ((hhw.x < f.ze.x) ? 1 : 0) | ((hhw.y < f.ze.y) ? 2 : 0);
+    const int d2 = lt2(mul2(sub2(f.he, f2(th)), sub2(f.hw, f2(th))), 0.f);
+    const int open = f.act & wet;
+    const int special = open & (d1a | d1b | d2);
+    float2 F = sel2(open & ~special, fm, f2(0.f));
+    if (__any_sync(0xffffffffu, special != 0)) {
+        const float sx = face_special(f.hw.x, f.he.x, f.zw.x, f.ze.x, th, g);
+        const float sy = face_special(f.hw.y, f.he.y, f.zw.y, f.ze.y, th, g);
+        F = sel2(special, make_float2(sx, sy), F);
+    }
+    return F;
 }
 
 /* ---------------- the row-marching step ---------------------------------- */
@@ -205,47 +269,62 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         S.dd[tid] = d;
     }
     __syncthreads();
-    const unsigned blk_bytes = 4u * RB * BW * 4u;
-    if (tid == 0) {
-        for (int b = 0; b < NS && b < nblk; b++) {
-            mbar_arrive_expect_tx(&S.bar[b], blk_bytes);
-            const int y = Ls + b * RB + M_H; /* padded row of the block's first row */
-            tma_load_2d(&S.stage[b][0][0][0], &P.tm_h[cur], c0, y, &S.bar[b]);
-            tma_load_2d(&S.stage[b][1][0][0], &P.tm_z, c0, y, &S.bar[b]);
-            tma_load_2d(&S.stage[b][2][0][0], &P.tm_qx[cur], c0, y, &S.bar[b]);
-            tma_load_2d(&S.stage[b][3][0][0], &P.tm_qy[cur], c0, y, &S.bar[b]);
-        }
-    }
+    const bool has_cls = P.cls != nullptr, has_rw = P.rainw != nullptr;
+    const unsigned blk_bytes = (unsigned)NF * RB * BW * 4u + (has_cls ? (unsigned)(M_CLSR * M_CLSW) : 0u) +
+                               (has_rw ? (unsigned)(M_RWR * BW * 4) : 0u);
+    /* block b holds rows Ls + b*RB .. +RB-1 of h, z, qx, qy, the Kahan
+     * compensation of the rows three above (the rows finished during b) and,
+     * when present, the class rows from two above and the rain weights from
+     * three above */
+    auto issue = [&](int b, int st) {
+        mbar_arrive_expect_tx(&S.bar[st], blk_bytes);
+        const int y = Ls + b * RB + M_H; /* padded row of the block's first row */
+        tma_load_2d(&S.stage[st][0][0][0], &P.tm_h[cur], c0, y, &S.bar[st]);
+        tma_load_2d(&S.stage[st][1][0][0], &P.tm_z, c0, y, &S.bar[st]);
+        tma_load_2d(&S.stage[st][2][0][0], &P.tm_qx[cur], c0, y, &S.bar[st]);
+        tma_load_2d(&S.stage[st][3][0][0], &P.tm_qy[cur], c0, y, &S.bar[st]);
+        tma_load_2d(&S.stage[st][4][0][0], &P.tm_kc, c0, y - 3, &S.bar[st]);
+        if (has_cls) tma_load_2d(&S.cls[st].v[0][0], &P.tm_cls, c0, y - 2, &S.bar[st]);
+        if (has_rw) tma_load_2d(&S.rw[st].v[0][0], &P.tm_rw, c0, y - 3, &S.bar[st]);
+    };
+    if (tid == 0)
+        for (int b = 0; b < NS && b < nblk; b++) issue(b, b);
 
     /* lane geometry: staged columns sc, sc+1; global columns cg, cg+1 */
     const int sc = warp * M_SW + 2 * lane;
     const int cg = c0 - M_H + sc;
     const bool own0 = (lane >= 2 && lane < 30) && cg < C;
     const bool own1 = (lane >= 2 && lane < 30) && cg + 1 < C;
+    const int ownm = (own0 ? 1 : 0) | (own1 ? 2 : 0);
     const int creg0 = sc < M_H ? 0 : (sc >= M_H + M_CW ? 2 : 1);
     const int creg1 = sc + 1 < M_H ? 0 : (sc + 1 >= M_H + M_CW ? 2 : 1);
-    /* datum shifts of the lane's two columns for rows above / inside / below the segment */
-    const float dzt0 = S.dd[creg0], dzm0 = S.dd[3 + creg0], dzb0 = S.dd[6 + creg0];
-    const float dzt1 = S.dd[creg1], dzm1 = S.dd[3 + creg1], dzb1 = S.dd[6 + creg1];
-    const float th = P.th, gg = P.g, rdx = P.rdx, rdy = P.rdy;
-    const float dt2 = sl.dt2, dt2dx = sl.dt2dx, dt2dy = sl.dt2dy, hdt2 = 0.5f * sl.dt2;
+    const float th = P.th, gg = P.g;
+    const float dt2 = sl.dt2, dt2dx = sl.dt2dx, dt2dy = sl.dt2dy;
     const float gdx = gg * dt2dx, gdy = gg * dt2dy;
-    const bool has_cls = P.cls != nullptr, has_rw = P.rainw != nullptr;
-    const float n_uni = S.ntab[0], gn2_uni = gg * n_uni * n_uni;
-    const bool col0_0 = (cg == 0), col0_1 = (cg + 1 == 0);
+    const float2 rdxy = make_float2(P.rdx, P.rdy);
+    const float n_uni = S.ntab[0];
+    const float fr_scale = -0.5f * dt2 * gg;          /* an = fr_scale * n^2 * sq * hm^-4/3 */
+    const float fr_uni = fr_scale * n_uni * n_uni;
+    /* source terms: rain rate * runoff fraction, evaporation on lake cells */
+    const float ewl = P.ev_wl_min;
+    const float rl1 = sl.rr1 * P.pct_lake, rd1 = sl.rr1 * P.pct_land;
+    const float rl2 = sl.rr2 * P.pct_lake, rd2 = sl.rr2 * P.pct_land;
+    const float ev1 = sl.ev1, ev2 = sl.ev2;
+    /* the cross convection of x faces vanishes on column 0 (SW2D-EFDC.cu:164) */
+    const float2 colm = make_float2(cg == 0 ? 0.f : 1.f, cg + 1 == 0 ? 0.f : 1.f);
 
     /* register windows, slot = (row - Ls) & 3 */
-    float2 H[4], Z[4], QX[4], QY[4], U[4], V[4], FX[4], FY[4];
-    float2 HL[4], ZL[4], UL[4], VR[4], FYR[4], RW[4], NN[4], NL[4], EX[4], GY[4];
-    int DRY[4];
+    float2 H[4], Z[4], QX[4], QY[4], U[4], UU[4], V[4], VV[4], VR[4];
+    float2 HL[4], ZL[4], EX[4], GY[4], FX[4], FY[4], FYR[4];
+    int ACT[4], ACTL[4], DRY[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        H[k] = Z[k] = QX[k] = QY[k] = U[k] = V[k] = FX[k] = FY[k] = make_float2(0.f, 0.f);
-        HL[k] = ZL[k] = UL[k] = VR[k] = FYR[k] = NN[k] = NL[k] = EX[k] = GY[k] = make_float2(0.f, 0.f);
-        RW[k] = make_float2(1.f, 1.f);
-        DRY[k] = 0;
+        H[k] = Z[k] = QX[k] = QY[k] = U[k] = UU[k] = V[k] = VV[k] = VR[k] = f2(0.f);
+        HL[k] = ZL[k] = EX[k] = GY[k] = FX[k] = FY[k] = FYR[k] = f2(0.f);
+        ACT[k] = ACTL[k] = DRY[k] = 0;
     }
-    float clamp = 0.f, qout = 0.f, rainacc = 0.f, evc = 0.f, sxm = 0.f, sym = 0.f;
+    float clamp = 0.f, qout = 0.f, rainacc = 0.f, evc = 0.f;
+    float sxm = 0.f, sym = 0.f;
 
     for (int b = 0; b < nblk; b++) {
         const int st = b % NS;
@@ -270,198 +349,188 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         const float* sz = &S.stage[st][1][0][0];
         const float* sqx = &S.stage[st][2][0][0];
         const float* sqy = &S.stage[st][3][0][0];
+        const float* skc = &S.stage[st][4][0][0];
+        const unsigned char* scl = &S.cls[st].v[0][0];
+        const float* srw = &S.rw[st].v[0][0];
 #pragma unroll
         for (int j = 0; j < RB; j++) {
             const int L = Ls + b * RB + j;
             const int s0 = j & 3, s1 = (j + 3) & 3, s2 = (j + 2) & 3, s3 = (j + 1) & 3; /* L, L-1, L-2, L-3 */
             /* ---- row L from the staged block ---- */
-            H[s0] = *reinterpret_cast<const float2*>(sh + j * BW + sc);
-            float2 zz = *reinterpret_cast<const float2*>(sz + j * BW + sc);
-            zz.x += L < rs ? dzt0 : (L >= re ? dzb0 : dzm0);
-            zz.y += L < rs ? dzt1 : (L >= re ? dzb1 : dzm1);
-            Z[s0] = zz;
-            QX[s0] = *reinterpret_cast<const float2*>(sqx + j * BW + sc);
-            QY[s0] = *reinterpret_cast<const float2*>(sqy + j * BW + sc);
-            const bool rowin = (L >= -M_H && L < R + M_H) && cg + M_H >= 0 && cg + M_H + 1 < Pp;
-            const size_t gL = (size_t)(L + M_H) * Pp + (cg + M_H);
-            if (has_cls) {
-                float2 nn = make_float2(n_uni, n_uni);
-                if (rowin) {
-                    const uchar2 cc = *reinterpret_cast<const uchar2*>(P.cls + gL);
-                    nn = make_float2(S.ntab[cc.x & 63], S.ntab[cc.y & 63]);
-                }
-                NN[s0] = nn;
-                NL[s0] = left2(nn);
+            const float2 h0 = *reinterpret_cast<const float2*>(sh + j * BW + sc);
+            /* datum shift of the lane's two columns for rows above / inside / below the segment */
+            const int dzr = L < rs ? 0 : (L >= re ? 6 : 3);
+            const float2 z0 = add2(*reinterpret_cast<const float2*>(sz + j * BW + sc),
+                                   make_float2(S.dd[dzr + creg0], S.dd[dzr + creg1]));
+            const float2 qx0 = *reinterpret_cast<const float2*>(sqx + j * BW + sc);
+            const float2 qy0 = *reinterpret_cast<const float2*>(sqy + j * BW + sc);
+            H[s0] = h0;
+            Z[s0] = z0;
+            QX[s0] = qx0;
+            QY[s0] = qy0;
+            ACT[s0] = act2(z0);
+            const float2 hl = left2(h0);
+            HL[s0] = hl;
+            ZL[s0] = left2(z0);
+            ACTL[s0] = leftbits(ACT[s0]);
+            /* ---- face velocities of row L (uu1 at the x face north, vv1 at the y face west) ---- */
+            const float2 hm = (L == R) ? H[s1] : mul2(add2(h0, H[s1]), f2(0.5f));
+            const float2 hn = mul2(add2(h0, hl), f2(0.5f));
+            const int okm = ge2(hm, th), okn = ge2(hn, th);
+            const float2 u = sel2(okm, mul2(qx0, rcp2(hm)), f2(0.f));
+            const float2 v = sel2(okn, mul2(qy0, rcp2(hn)), f2(0.f));
+            U[s0] = u;
+            V[s0] = v;
+            const float2 ul = left2(u), vr = right2(v);
+            UU[s0] = add2(u, ul);
+            VV[s0] = add2(v, vr);
+            VR[s0] = vr;
+            /* CFL face speeds (|velocity| + sqrt(g h)) of the owned faces */
+            if (L >= rs && L < re) {
+                const float2 cx = add2(abs2(u), sqrt2(mul2(f2(gg), hm)));
+                const float2 cy = add2(abs2(v), sqrt2(mul2(f2(gg), hn)));
+                const int mx = okm & ownm & ACT[s0] & ACT[s1];
+                const int my = okn & ownm & ACT[s0] & ACTL[s0];
+                sxm = fmaxf(sxm, fmaxf((mx & 1) ? cx.x : 0.f, (mx & 2) ? cx.y : 0.f));
+                sym = fmaxf(sym, fmaxf((my & 1) ? cy.x : 0.f, (my & 2) ? cy.y : 0.f));
             }
-            if (has_rw) RW[s0] = rowin ? *reinterpret_cast<const float2*>(P.rainw + gL) : make_float2(1.f, 1.f);
-            HL[s0] = left2(H[s0]);
-            ZL[s0] = left2(Z[s0]);
-            /* ---- face velocities of row L and CFL face speeds of owned faces ---- */
-            const bool rowown = (L >= rs && L < re);
-#pragma unroll
-            for (int k = 0; k < 2; k++) {
-                const float hLk = comp(H[s0], k);
-                const float hm = (L == R) ? comp(H[s1], k) : 0.5f * (hLk + comp(H[s1], k));
-                const float u = (hm >= th) ? comp(QX[s0], k) * frcp(hm) : 0.f;
-                setc(U[s0], k, u);
-                const float hn = 0.5f * (hLk + comp(HL[s0], k));
-                const float v = (hn >= th) ? comp(QY[s0], k) * frcp(hn) : 0.f;
-                setc(V[s0], k, v);
-                const bool own = (k ? own1 : own0) && rowown;
-                const bool za = is_act(comp(Z[s0], k));
-                const bool okx = own && hm >= th && za && is_act(comp(Z[s1], k));
-                const bool oky = own && hn >= th && za && is_act(comp(ZL[s0], k));
-                sxm = fmaxf(sxm, okx ? (fabsf(u) + fsqrt(gg * hm)) * rdx : 0.f);
-                sym = fmaxf(sym, oky ? (fabsf(v) + fsqrt(gg * hn)) * rdy : 0.f);
-            }
-            UL[s0] = left2(U[s0]);
-            VR[s0] = right2(V[s0]);
-            /* ---- edge terms: along x between x faces L-1 and L, cross for y faces
-             *      between rows L-1 and L, and the two edge kinds of row L-1 ---- */
-            const float2 qxr = right2(QX[s1]), qyr = right2(QY[s1]);
-            float2 EY, GX;
-#pragma unroll
-            for (int k = 0; k < 2; k++) {
-                setc(EX[s1], k, edge_term(0.25f * (comp(U[s0], k) + comp(U[s1], k)), comp(QX[s1], k), comp(QX[s0], k)));
-                setc(GY[s1], k, edge_term(0.25f * (comp(U[s0], k) + comp(UL[s0], k)), comp(QY[s1], k), comp(QY[s0], k)));
-                setc(EY, k, edge_term(0.25f * (comp(VR[s1], k) + comp(V[s1], k)), comp(QY[s1], k), comp(qyr, k)));
-                setc(GX, k, edge_term(0.25f * (comp(VR[s1], k) + comp(VR[s2], k)), comp(QX[s1], k), comp(qxr, k)));
-            }
-            const float2 EYL = left2(EY), GXL = left2(GX);
+            /* ---- edge terms of the convection ---- */
+            EX[s1] = edge2(mul2(add2(u, U[s1]), f2(0.25f)), QX[s1], qx0);
+            GY[s1] = edge2(mul2(UU[s0], f2(0.25f)), QY[s1], qy0);
+            const float2 EY = edge2(mul2(VV[s1], f2(0.25f)), QY[s1], right2(QY[s1]));
+            const float2 GX = edge2(mul2(add2(VR[s1], VR[s2]), f2(0.25f)), QX[s1], right2(QX[s1]));
             /* ---- face discharges of row L-1 ---- */
             const int rf = L - 1;
-#pragma unroll
-            for (int k = 0; k < 2; k++) {
-                FaceIn fx;
-                fx.hw = comp(H[s2], k);
-                fx.he = comp(H[s1], k);
-                fx.zw = comp(Z[s2], k);
-                fx.ze = comp(Z[s1], k);
-                fx.q0 = comp(QX[s1], k);
-                fx.u0 = comp(U[s1], k);
-                fx.vt = 0.25f * (comp(V[s1], k) + comp(V[s2], k) + comp(VR[s1], k) + comp(VR[s2], k));
-                fx.along = dt2dx * (comp(EX[s1], k) - comp(EX[s2], k));
-                fx.across = (k ? col0_1 : col0_0) ? 0.f : dt2dy * (comp(GX, k) - comp(GXL, k));
-                fx.gdt2n = gdx;
-                if (has_cls) {
-                    const float nf = 0.5f * (comp(NN[s1], k) + comp(NN[s2], k));
-                    fx.gn2 = gg * nf * nf;
+            {
+                Face2 f;
+                f.hw = H[s2];
+                f.he = H[s1];
+                f.zw = Z[s2];
+                f.ze = Z[s1];
+                f.act = ACT[s2] & ACT[s1];
+                f.q0 = QX[s1];
+                f.u0 = U[s1];
+                f.vt = mul2(add2(VV[s1], VV[s2]), f2(0.25f));
+                f.conv = fma2(sub2(EX[s1], EX[s2]), f2(dt2dx), mul2(mul2(sub2(GX, left2(GX)), f2(dt2dy)), colm));
+                if (has_cls) { /* face n = mean of the two cells' n; class rows L-2, L-1 at j, j+1 */
+                    const unsigned char* c1 = scl + (j + 1) * M_CLSW + sc;
+                    const unsigned char* c2 = scl + j * M_CLSW + sc;
+                    const float2 nf = mul2(add2(make_float2(S.ntab[c1[0] & 63], S.ntab[c1[1] & 63]),
+                                                make_float2(S.ntab[c2[0] & 63], S.ntab[c2[1] & 63])),
+                                           f2(0.5f));
+                    f.fr = mul2(mul2(nf, nf), f2(fr_scale));
                 } else {
-                    fx.gn2 = gn2_uni;
+                    f.fr = f2(fr_uni);
                 }
-                float F = face_flux(fx, th, gg, hdt2);
+                float2 F = face_flux2(f, th, gg, gdx);
                 if (rf == R) { /* south edge: free overfall when open (SW2D-EFDC.cu:131 law) */
-                    const float hw = fx.hw;
-                    F = (P.outflow_south && is_act(fx.zw) && hw > th) ? 0.5440f * hw * fsqrt(gg * hw) : 0.f;
+                    const float2 hw = f.hw;
+                    const int m = P.outflow_south ? (ACT[s2] & gt2(hw, th)) : 0;
+                    F = sel2(m, mul2(mul2(f2(0.5440f), hw), sqrt2(mul2(f2(gg), hw))), f2(0.f));
                 }
-                setc(FX[s1], k, F);
-                FaceIn fy;
-                fy.hw = comp(HL[s1], k);
-                fy.he = comp(H[s1], k);
-                fy.zw = comp(ZL[s1], k);
-                fy.ze = comp(Z[s1], k);
-                fy.q0 = comp(QY[s1], k);
-                fy.u0 = comp(V[s1], k);
-                fy.vt = 0.25f * (comp(U[s1], k) + comp(U[s0], k) + comp(UL[s1], k) + comp(UL[s0], k));
-                fy.along = dt2dy * (comp(EY, k) - comp(EYL, k));
-                fy.across = (rf == 0) ? 0.f : dt2dx * (comp(GY[s1], k) - comp(GY[s2], k));
-                fy.gdt2n = gdy;
-                if (has_cls) {
-                    const float nf = 0.5f * (comp(NN[s1], k) + comp(NL[s1], k));
-                    fy.gn2 = gg * nf * nf;
+                FX[s1] = F;
+            }
+            {
+                Face2 f;
+                f.hw = HL[s1];
+                f.he = H[s1];
+                f.zw = ZL[s1];
+                f.ze = Z[s1];
+                f.act = ACTL[s1] & ACT[s1];
+                f.q0 = QY[s1];
+                f.u0 = V[s1];
+                f.vt = mul2(add2(UU[s1], UU[s0]), f2(0.25f));
+                const float2 along = mul2(sub2(EY, left2(EY)), f2(dt2dy));
+                f.conv = (rf == 0) ? along : fma2(sub2(GY[s1], GY[s2]), f2(dt2dx), along);
+                if (has_cls) { /* row L-1, columns c-1, c, c+1 (sc >= 0 and row j+1 >= 1 keep c-1 inside) */
+                    const unsigned char* c1 = scl + (j + 1) * M_CLSW + sc;
+                    const float nl = S.ntab[c1[-1] & 63], n0 = S.ntab[c1[0] & 63], n1 = S.ntab[c1[1] & 63];
+                    const float2 nf = mul2(add2(make_float2(n0, n1), make_float2(nl, n0)), f2(0.5f));
+                    f.fr = mul2(mul2(nf, nf), f2(fr_scale));
                 } else {
-                    fy.gn2 = gn2_uni;
+                    f.fr = f2(fr_uni);
                 }
-                setc(FY[s1], k, face_flux(fy, th, gg, hdt2));
+                FY[s1] = face_flux2(f, th, gg, gdy);
             }
             /* ---- provisional depth of row L-2 -> dry flags ---- */
             FYR[s2] = right2(FY[s2]);
             {
-                int dry = 0;
-#pragma unroll
-                for (int k = 0; k < 2; k++) {
-                    const float ho = comp(H[s2], k);
-                    const bool lake = ho > P.ev_wl_min;
-                    const float pct = lake ? P.pct_lake : P.pct_land;
-                    const float ev = lake ? sl.ev1 : 0.f;
-                    const float hs = ho - dt2 * ((comp(FX[s1], k) - comp(FX[s2], k)) * rdx +
-                                                 (comp(FYR[s2], k) - comp(FY[s2], k)) * rdy -
-                                                 sl.rr1 * comp(RW[s2], k) * pct + ev);
-                    dry |= (is_act(comp(Z[s2], k)) && hs < th) ? (1 << k) : 0;
-                }
-                DRY[s2] = dry;
+                const float2 ho = H[s2];
+                const int lake = gt2(ho, ewl);
+                float2 src = sel2(lake, make_float2(rl1, rl1), make_float2(rd1, rd1));
+                if (has_rw) src = mul2(src, *reinterpret_cast<const float2*>(srw + (j + 1) * BW + sc));
+                src = sub2(src, sel2(lake, f2(ev1), f2(0.f)));
+                const float2 div = fma2(sub2(FX[s1], FX[s2]), f2(rdxy.x), mul2(sub2(FYR[s2], FY[s2]), f2(rdxy.y)));
+                const float2 hs = fma2(sub2(div, src), f2(-dt2), ho);
+                DRY[s2] = ACT[s2] & lt2(hs, th);
             }
             /* ---- final depth of row L-3 ---- */
-            {
-                const int r = L - 3;
+            const int r = L - 3;
+            if (r >= rs && r < re) {
                 const int dc = DRY[s3], dN = DRY[s0], dS = DRY[s2];
-                const int dW = leftbits(dc), dE = rightbits(dc);
-                if (r >= rs && r < re && (own0 || own1)) {
-                    const size_t g = (size_t)(r + M_H) * Pp + (cg + M_H);
-                    const float2 kcv = own1 ? *reinterpret_cast<const float2*>(P.kc + g) : make_float2(P.kc[g], 0.f);
-                    float2 hout, kout, fNo, fWo, fSo;
-#pragma unroll
-                    for (int k = 0; k < 2; k++) {
-                        float fN = comp(FX[s3], k), fS = comp(FX[s2], k), fW = comp(FY[s3], k), fE = comp(FYR[s3], k);
-                        const int bc = (dc >> k) & 1;
-                        fN = ((fN > 0.f && ((dN >> k) & 1)) || (fN < 0.f && bc)) ? 0.f : fN;
-                        fS = ((fS > 0.f && bc) || (fS < 0.f && ((dS >> k) & 1))) ? 0.f : fS;
-                        fW = ((fW > 0.f && ((dW >> k) & 1)) || (fW < 0.f && bc)) ? 0.f : fW;
-                        fE = ((fE > 0.f && bc) || (fE < 0.f && ((dE >> k) & 1))) ? 0.f : fE;
-                        const bool own = k ? own1 : own0;
-                        const bool act = is_act(comp(Z[s3], k));
-                        const float ho = comp(H[s3], k);
-                        const float wgt = comp(RW[s3], k);
-                        const bool lake = ho > P.ev_wl_min;
-                        const float pct = lake ? P.pct_lake : P.pct_land;
-                        const float ev = lake ? sl.ev2 : 0.f;
-                        const float dh = -dt2 * ((fS - fN) * rdx + (fE - fW) * rdy - sl.rr2 * wgt * pct + ev);
-                        /* Kahan: the increment is small against the depth */
-                        const float y = dh - comp(kcv, k);
-                        const float t = ho + y;
-                        float kc = (t - ho) - y;
-                        float hn = t;
-                        if (own && act) {
-                            clamp += hn < 0.f ? -hn : 0.f;
-                            if (P.ledger_cells) {
-                                rainacc += wgt * pct;
-                                evc += lake ? 1.f : 0.f;
-                            }
-                            if (r == R - 1) qout += fS;
-                        }
-                        kc = (act && hn >= 0.f) ? kc : 0.f;
-                        hn = act ? fmaxf(hn, 0.f) : 0.f;
-                        setc(hout, k, hn);
-                        setc(kout, k, kc);
-                        setc(fNo, k, fN);
-                        setc(fWo, k, fW);
-                        setc(fSo, k, fS);
-                    }
-                    if (own0 && own1) {
-                        *reinterpret_cast<float2*>(P.h[nxt] + g) = hout;
-                        *reinterpret_cast<float2*>(P.kc + g) = kout;
-                        *reinterpret_cast<float2*>(P.qx[nxt] + g) = fNo;
-                        *reinterpret_cast<float2*>(P.qy[nxt] + g) = fWo;
-                        if (r == R - 1) *reinterpret_cast<float2*>(P.qx[nxt] + g + Pp) = fSo;
-                    } else {
-                        P.h[nxt][g] = hout.x;
-                        P.kc[g] = kout.x;
-                        P.qx[nxt][g] = fNo.x;
-                        P.qy[nxt][g] = fWo.x;
-                        if (r == R - 1) P.qx[nxt][g + Pp] = fSo.x;
-                    }
+                float2 fN = FX[s3], fS = FX[s2], fW = FY[s3], fE = FYR[s3];
+                if (__any_sync(0xffffffffu, (dc | dN | dS) != 0)) {
+                    /* treat_error (SW2D-EFDC.cu:695-725): no outflow from a dry cell */
+                    const int dW = leftbits(dc), dE = rightbits(dc);
+                    const int zN = (gt2(fN, 0.f) & dN) | (lt2(fN, 0.f) & dc);
+                    const int zS = (gt2(fS, 0.f) & dc) | (lt2(fS, 0.f) & dS);
+                    const int zW = (gt2(fW, 0.f) & dW) | (lt2(fW, 0.f) & dc);
+                    const int zE = (gt2(fE, 0.f) & dc) | (lt2(fE, 0.f) & dE);
+                    fN = sel2(zN, f2(0.f), fN);
+                    fS = sel2(zS, f2(0.f), fS);
+                    fW = sel2(zW, f2(0.f), fW);
+                    fE = sel2(zE, f2(0.f), fE);
+                }
+                const float2 ho = H[s3];
+                const int act = ACT[s3];
+                const int lake = gt2(ho, ewl);
+                float2 src = sel2(lake, f2(rl2), f2(rd2));
+                const float2 wgt = has_rw ? *reinterpret_cast<const float2*>(srw + j * BW + sc) : f2(1.f);
+                if (has_rw) src = mul2(src, wgt);
+                src = sub2(src, sel2(lake, f2(ev2), f2(0.f)));
+                const float2 div = fma2(sub2(fS, fN), f2(rdxy.x), mul2(sub2(fE, fW), f2(rdxy.y)));
+                const float2 dh = mul2(sub2(div, src), f2(-dt2));
+                /* Kahan: the increment is small against the depth */
+                const float2 kc0 = *reinterpret_cast<const float2*>(skc + j * BW + sc);
+                const float2 y = sub2(dh, kc0);
+                const float2 t = add2(ho, y);
+                float2 kc = sub2(sub2(t, ho), y);
+                const int pos = ge2(t, 0.f);
+                const int oa = ownm & act;
+                {
+                    const int neg = oa & ~pos;
+                    clamp -= ((neg & 1) ? t.x : 0.f) + ((neg & 2) ? t.y : 0.f);
+                }
+                if (P.ledger_cells) {
+                    float2 pw = sel2(lake, f2(P.pct_lake), f2(P.pct_land));
+                    if (has_rw) pw = mul2(pw, wgt);
+                    rainacc += ((oa & 1) ? pw.x : 0.f) + ((oa & 2) ? pw.y : 0.f);
+                    const int ol = oa & lake;
+                    evc += (float)((ol & 1) + (ol >> 1));
+                }
+                if (r == R - 1) qout += ((oa & 1) ? fS.x : 0.f) + ((oa & 2) ? fS.y : 0.f);
+                kc = sel2(act & pos, kc, f2(0.f));
+                const float2 hout = sel2(act, make_float2(fmaxf(t.x, 0.f), fmaxf(t.y, 0.f)), f2(0.f));
+                const size_t g = (size_t)(r + M_H) * Pp + (cg + M_H);
+                if (own1) {
+                    *reinterpret_cast<float2*>(P.h[nxt] + g) = hout;
+                    *reinterpret_cast<float2*>(P.kc + g) = kc;
+                    *reinterpret_cast<float2*>(P.qx[nxt] + g) = fN;
+                    *reinterpret_cast<float2*>(P.qy[nxt] + g) = fW;
+                    if (r == R - 1) *reinterpret_cast<float2*>(P.qx[nxt] + g + Pp) = fS;
+                } else if (own0) {
+                    P.h[nxt][g] = hout.x;
+                    P.kc[g] = kc.x;
+                    P.qx[nxt][g] = fN.x;
+                    P.qy[nxt][g] = fW.x;
+                    if (r == R - 1) P.qx[nxt][g + Pp] = fS.x;
                 }
             }
         }
         __syncthreads(); /* every warp is done with block b */
         if (tid == 0 && b + NS < nblk) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive_expect_tx(&S.bar[st], blk_bytes);
-            const int y = Ls + (b + NS) * RB + M_H;
-            tma_load_2d(&S.stage[st][0][0][0], &P.tm_h[cur], c0, y, &S.bar[st]);
-            tma_load_2d(&S.stage[st][1][0][0], &P.tm_z, c0, y, &S.bar[st]);
-            tma_load_2d(&S.stage[st][2][0][0], &P.tm_qx[cur], c0, y, &S.bar[st]);
-            tma_load_2d(&S.stage[st][3][0][0], &P.tm_qy[cur], c0, y, &S.bar[st]);
+            issue(b + NS, st);
         }
     }
 
@@ -495,8 +564,8 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
             mx = fmaxf(mx, S.redf[k][0]);
             my = fmaxf(my, S.redf[k][1]);
         }
-        pr.sx = mx;
-        pr.sy = my;
+        pr.sx = mx * rdxy.x; /* rdx > 0: the maximum commutes with the scaling */
+        pr.sy = my * rdxy.y;
         part[blockIdx.x] = pr;
     }
 }

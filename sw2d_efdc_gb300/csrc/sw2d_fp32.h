@@ -28,8 +28,11 @@ constexpr int M_SW = 56;               /* output columns per warp (2 per lane, l
 constexpr int M_CW = M_NW * M_SW;      /* 224 output columns per strip */
 constexpr int M_BW = M_CW + 2 * M_H;   /* 232 staged columns */
 constexpr int M_RB = 4;                /* rows per staged block (TMA box height) */
-constexpr int M_NS = 3;                /* blocks in the staging ring */
+constexpr int M_NS = 2;                /* blocks in the staging ring */
 constexpr int M_NT = M_NW * 32;
+constexpr int M_CLSW = 240;            /* staged Manning-class columns (bytes; a multiple of 16) */
+constexpr int M_CLSR = M_RB + 2;       /* class rows per block: the block's rows and the two above */
+constexpr int M_RWR = M_RB + 1;        /* rain-weight rows per block: from three rows above the block */
 constexpr int T32_MAXCLASS = 64;
 
 /* Length and forcing of a scenario's next iteration, written by the
@@ -66,7 +69,8 @@ struct Part32 {
 };
 
 struct Scn32 {
-    CUtensorMap tm_h[2], tm_qx[2], tm_qy[2], tm_z;
+    CUtensorMap tm_h[2], tm_qx[2], tm_qy[2], tm_z, tm_kc;
+    CUtensorMap tm_cls, tm_rw;   /* set when the scenario has a class raster / a rain-weight field */
     float* h[2];
     float* qx[2];
     float* qy[2];
