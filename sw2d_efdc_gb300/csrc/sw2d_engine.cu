@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 
@@ -80,6 +81,10 @@ int Engine32::init(std::string* err) {
     if (fp32_configure_kernels() != 0) {
         if (err) *err = "cannot enable the FP32 kernel's shared memory";
         return SW2D_ERR_CUDA;
+    }
+    /* rows per work item: SW2D_SEGMENT_ROWS overrides the default (tuning knob) */
+    if (seg_rows_ == 0) {
+        if (const char* e = std::getenv("SW2D_SEGMENT_ROWS")) seg_rows_ = std::max(0, std::atoi(e));
     }
     if (!encode_fn()) {
         if (err) *err = "cuTensorMapEncodeTiled unavailable";
@@ -329,13 +334,19 @@ int Engine32::rebuild(std::string* err) {
     if (!dirty_) return SW2D_OK;
     work_.clear();
     std::vector<Scn32> host(scn_.size());
-    for (size_t i = 0; i < scn_.size(); i++) {
-        Scn32& d = scn_[i]->d;
-        d.first_work = (int)work_.size();
-        for (int ty = 0; ty < d.tiles_y; ty++)
-            for (int tx = 0; tx < d.tiles_x; tx++) work_.push_back(make_int4((int)i, tx, ty, 0));
-        d.nwork = (int)work_.size() - d.first_work;
-        host[i] = d;
+    /* work items grouped by feature class, scenarios in order within a class */
+    for (int k = 0; k < T32_NCLASS; k++) {
+        class_first_[k] = (int)work_.size();
+        for (size_t i = 0; i < scn_.size(); i++) {
+            Scn32& d = scn_[i]->d;
+            if (fp32_feature_class(d) != k) continue;
+            d.first_work = (int)work_.size();
+            for (int ty = 0; ty < d.tiles_y; ty++)
+                for (int tx = 0; tx < d.tiles_x; tx++) work_.push_back(make_int4((int)i, tx, ty, 0));
+            d.nwork = (int)work_.size() - d.first_work;
+            host[i] = d;
+        }
+        class_n_[k] = (int)work_.size() - class_first_[k];
     }
     if (host.size() > d_scn_cap_) {
         cudaFree(d_scn_);
@@ -370,7 +381,7 @@ int Engine32::build_graph(std::string* err) {
     cudaGraph_t g;
     ECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < kChunk32; k++)
-        fp32_launch_iteration(d_scn_, (int)scn_.size(), d_work_, (int)work_.size(), d_part_, stream_);
+        fp32_launch_iteration(d_scn_, (int)scn_.size(), d_work_, class_first_, class_n_, d_part_, stream_);
     ECK(cudaStreamEndCapture(stream_, &g));
     cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
     cudaGraphDestroy(g);
@@ -407,7 +418,7 @@ int Engine32::run(long long n, std::string* err) {
     ECK(cudaEventRecord(ev_a_, stream_));
     for (long long k = 0; k < n / kChunk32; k++) ECK(cudaGraphLaunch(graph_, stream_));
     for (long long k = 0; k < n % kChunk32; k++)
-        fp32_launch_iteration(d_scn_, (int)scn_.size(), d_work_, (int)work_.size(), d_part_, stream_);
+        fp32_launch_iteration(d_scn_, (int)scn_.size(), d_work_, class_first_, class_n_, d_part_, stream_);
     ECK(cudaGetLastError());
     ECK(cudaEventRecord(ev_b_, stream_));
     ECK(cudaEventSynchronize(ev_b_));

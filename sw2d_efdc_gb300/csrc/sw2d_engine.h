@@ -77,6 +77,7 @@ class Engine32 {
     cudaStream_t stream_ = nullptr;
     std::vector<std::unique_ptr<Scenario32>> scn_;
     std::vector<int4> work_;
+    int class_first_[T32_NCLASS] = {}, class_n_[T32_NCLASS] = {}; /* work ranges per feature class */
     Scn32* d_scn_ = nullptr;
     size_t d_scn_cap_ = 0;
     int4* d_work_ = nullptr;

@@ -138,14 +138,27 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b
 __device__ __forceinline__ float2 abs2(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
 __device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(rcpa(a.x), rcpa(a.y)); }
 __device__ __forceinline__ float2 sqrt2(float2 a) { return make_float2(sqrta(a.x), sqrta(a.y)); }
-/* m: bit 0 selects a.x, bit 1 selects a.y; else b */
-__device__ __forceinline__ float2 sel2(int m, float2 a, float2 b) {
-    return make_float2((m & 1) ? a.x : b.x, (m & 2) ? a.y : b.y);
-}
-__device__ __forceinline__ int ge2(float2 a, float t) { return (a.x >= t ? 1 : 0) | (a.y >= t ? 2 : 0); }
-__device__ __forceinline__ int gt2(float2 a, float t) { return (a.x > t ? 1 : 0) | (a.y > t ? 2 : 0); }
-__device__ __forceinline__ int lt2(float2 a, float t) { return (a.x < t ? 1 : 0) | (a.y < t ? 2 : 0); }
-__device__ __forceinline__ int act2(float2 z) { return (is_act(z.x) ? 1 : 0) | (is_act(z.y) ? 2 : 0); }
+/* |a| * b and |a| + b per column (the absolute value rides on the scalar
+ * instruction's operand modifier) */
+__device__ __forceinline__ float2 absmul2(float2 a, float2 b) { return make_float2(fabsf(a.x) * b.x, fabsf(a.y) * b.y); }
+__device__ __forceinline__ float2 absadd2(float2 a, float2 b) { return make_float2(fabsf(a.x) + b.x, fabsf(a.y) + b.y); }
+
+/* a condition per column; the rows' activity and dry flags travel between
+ * rows as 2-bit ints (bit k = column k) */
+struct B2 {
+    bool x, y;
+};
+__device__ __forceinline__ B2 operator&(B2 a, B2 b) { return {a.x && b.x, a.y && b.y}; }
+__device__ __forceinline__ B2 operator|(B2 a, B2 b) { return {a.x || b.x, a.y || b.y}; }
+__device__ __forceinline__ B2 andnot(B2 a, B2 b) { return {a.x && !b.x, a.y && !b.y}; }
+__device__ __forceinline__ B2 bits2(int m) { return {(m & 1) != 0, (m & 2) != 0}; }
+__device__ __forceinline__ int mask2(B2 m) { return (m.x ? 1 : 0) | (m.y ? 2 : 0); }
+__device__ __forceinline__ bool any2(B2 m) { return m.x || m.y; }
+__device__ __forceinline__ float2 sel2(B2 m, float2 a, float2 b) { return make_float2(m.x ? a.x : b.x, m.y ? a.y : b.y); }
+__device__ __forceinline__ B2 ge2(float2 a, float t) { return {a.x >= t, a.y >= t}; }
+__device__ __forceinline__ B2 gt2(float2 a, float t) { return {a.x > t, a.y > t}; }
+__device__ __forceinline__ B2 lt2(float2 a, float t) { return {a.x < t, a.y < t}; }
+__device__ __forceinline__ B2 act2(float2 z) { return {is_act(z.x), is_act(z.y)}; }
 
 /* hm^-1.3333330 = 2^(-1.3333330 log2 hm), the friction power (SW2D-EFDC.cu:193) */
 __device__ __forceinline__ float2 rpow_manning2(float2 hm) {
@@ -171,7 +184,7 @@ __device__ __forceinline__ int rightbits(int v) {
  * velocities, w (q1 + q0) + |w| (q0 - q1), q0 on the upstream-indexed face.
  * Each edge is shared by the two faces it separates, so it is computed once. */
 __device__ __forceinline__ float2 edge2(float2 w, float2 q0, float2 q1) {
-    return fma2(w, add2(q1, q0), mul2(abs2(w), sub2(q0, q1)));
+    return fma2(w, add2(q1, q0), absmul2(w, sub2(q0, q1)));
 }
 
 /* Weir and dry-bed discharges of one face (SW2D-EFDC.cu:125-157), for the
@@ -209,15 +222,15 @@ __device__ __forceinline__ float2 face_flux2(const Face2& f, float th, float g, 
     const float2 num = sub2(fma2(an, f.q0, f.q0), add2(f.conv, grav));
     const float2 fm = mul2(num, rcp2(sub2(f2(1.f), an)));
     /* which form applies (SW2D-EFDC.cu:115-165) */
-    const int wet = gt2(f.hw, th) | gt2(f.he, th);
+    const B2 wet = gt2(f.hw, th) | gt2(f.he, th);
     const float2 hhe = add2(f.he, f.ze), hhw = add2(f.hw, f.zw);
-    const int d1a = ((hhe.x < f.zw.x) ? 1 : 0) | ((hhe.y < f.zw.y) ? 2 : 0);
-    const int d1b = ((hhw.x < f.ze.x) ? 1 : 0) | ((hhw.y < f.ze.y) ? 2 : 0);
-    const int d2 = lt2(mul2(sub2(f.he, f2(th)), sub2(f.hw, f2(th))), 0.f);
-    const int open = f.act & wet;
-    const int special = open & (d1a | d1b | d2);
-    float2 F = sel2(open & ~special, fm, f2(0.f));
-    if (__any_sync(0xffffffffu, special != 0)) {
+    const B2 d1a = {hhe.x < f.zw.x, hhe.y < f.zw.y};
+    const B2 d1b = {hhw.x < f.ze.x, hhw.y < f.ze.y};
+    const B2 d2 = lt2(mul2(sub2(f.he, f2(th)), sub2(f.hw, f2(th))), 0.f);
+    const B2 open = bits2(f.act) & wet;
+    const B2 special = open & (d1a | d1b | d2);
+    float2 F = sel2(andnot(open, special), fm, f2(0.f));
+    if (__any_sync(0xffffffffu, any2(special))) {
         const float sx = face_special(f.hw.x, f.he.x, f.zw.x, f.ze.x, th, g);
         const float sy = face_special(f.hw.y, f.he.y, f.zw.y, f.ze.y, th, g);
         F = sel2(special, make_float2(sx, sy), F);
@@ -227,6 +240,10 @@ __device__ __forceinline__ float2 face_flux2(const Face2& f, float th, float g, 
 
 /* ---------------- the row-marching step ---------------------------------- */
 
+/* CLS: the scenario has a Manning-class raster; RW: a rain-weight field;
+ * LAKE: lake cells (depth > ev_wl_min) lose a different fraction of the rain
+ * than land cells (the per-cell ledger is then kept too). */
+template <bool CLS, bool RW, bool LAKE>
 __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scns, const int4* __restrict__ work,
                                                    Part32* __restrict__ part) {
     extern __shared__ unsigned char smem_raw[];
@@ -269,7 +286,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         S.dd[tid] = d;
     }
     __syncthreads();
-    const bool has_cls = P.cls != nullptr, has_rw = P.rainw != nullptr;
+    constexpr bool has_cls = CLS, has_rw = RW;
     const unsigned blk_bytes = (unsigned)NF * RB * BW * 4u + (has_cls ? (unsigned)(M_CLSR * M_CLSW) : 0u) +
                                (has_rw ? (unsigned)(M_RWR * BW * 4) : 0u);
     /* block b holds rows Ls + b*RB .. +RB-1 of h, z, qx, qy, the Kahan
@@ -310,6 +327,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
     const float rl1 = sl.rr1 * P.pct_lake, rd1 = sl.rr1 * P.pct_land;
     const float rl2 = sl.rr2 * P.pct_lake, rd2 = sl.rr2 * P.pct_land;
     const float ev1 = sl.ev1, ev2 = sl.ev2;
+    constexpr bool lakefx = LAKE;
     /* the cross convection of x faces vanishes on column 0 (SW2D-EFDC.cu:164) */
     const float2 colm = make_float2(cg == 0 ? 0.f : 1.f, cg + 1 == 0 ? 0.f : 1.f);
 
@@ -368,7 +386,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
             Z[s0] = z0;
             QX[s0] = qx0;
             QY[s0] = qy0;
-            ACT[s0] = act2(z0);
+            ACT[s0] = mask2(act2(z0));
             const float2 hl = left2(h0);
             HL[s0] = hl;
             ZL[s0] = left2(z0);
@@ -376,7 +394,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
             /* ---- face velocities of row L (uu1 at the x face north, vv1 at the y face west) ---- */
             const float2 hm = (L == R) ? H[s1] : mul2(add2(h0, H[s1]), f2(0.5f));
             const float2 hn = mul2(add2(h0, hl), f2(0.5f));
-            const int okm = ge2(hm, th), okn = ge2(hn, th);
+            const B2 okm = ge2(hm, th), okn = ge2(hn, th);
             const float2 u = sel2(okm, mul2(qx0, rcp2(hm)), f2(0.f));
             const float2 v = sel2(okn, mul2(qy0, rcp2(hn)), f2(0.f));
             U[s0] = u;
@@ -387,12 +405,10 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
             VR[s0] = vr;
             /* CFL face speeds (|velocity| + sqrt(g h)) of the owned faces */
             if (L >= rs && L < re) {
-                const float2 cx = add2(abs2(u), sqrt2(mul2(f2(gg), hm)));
-                const float2 cy = add2(abs2(v), sqrt2(mul2(f2(gg), hn)));
-                const int mx = okm & ownm & ACT[s0] & ACT[s1];
-                const int my = okn & ownm & ACT[s0] & ACTL[s0];
-                sxm = fmaxf(sxm, fmaxf((mx & 1) ? cx.x : 0.f, (mx & 2) ? cx.y : 0.f));
-                sym = fmaxf(sym, fmaxf((my & 1) ? cy.x : 0.f, (my & 2) ? cy.y : 0.f));
+                const float2 cx = sel2(okm & bits2(ownm & ACT[s0] & ACT[s1]), absadd2(u, sqrt2(mul2(f2(gg), hm))), f2(0.f));
+                const float2 cy = sel2(okn & bits2(ownm & ACT[s0] & ACTL[s0]), absadd2(v, sqrt2(mul2(f2(gg), hn))), f2(0.f));
+                sxm = fmaxf(sxm, fmaxf(cx.x, cx.y));
+                sym = fmaxf(sym, fmaxf(cy.x, cy.y));
             }
             /* ---- edge terms of the convection ---- */
             EX[s1] = edge2(mul2(add2(u, U[s1]), f2(0.25f)), QX[s1], qx0);
@@ -425,7 +441,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 float2 F = face_flux2(f, th, gg, gdx);
                 if (rf == R) { /* south edge: free overfall when open (SW2D-EFDC.cu:131 law) */
                     const float2 hw = f.hw;
-                    const int m = P.outflow_south ? (ACT[s2] & gt2(hw, th)) : 0;
+                    const B2 m = bits2(P.outflow_south ? ACT[s2] : 0) & gt2(hw, th);
                     F = sel2(m, mul2(mul2(f2(0.5440f), hw), sqrt2(mul2(f2(gg), hw))), f2(0.f));
                 }
                 FX[s1] = F;
@@ -456,38 +472,34 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
             FYR[s2] = right2(FY[s2]);
             {
                 const float2 ho = H[s2];
-                const int lake = gt2(ho, ewl);
-                float2 src = sel2(lake, make_float2(rl1, rl1), make_float2(rd1, rd1));
+                float2 src = f2(rd1);
+                B2 lake = {false, false};
+                if (lakefx) {
+                    lake = gt2(ho, ewl);
+                    src = sel2(lake, f2(rl1), src);
+                }
                 if (has_rw) src = mul2(src, *reinterpret_cast<const float2*>(srw + (j + 1) * BW + sc));
-                src = sub2(src, sel2(lake, f2(ev1), f2(0.f)));
+                if (lakefx) src = sub2(src, sel2(lake, f2(ev1), f2(0.f)));
                 const float2 div = fma2(sub2(FX[s1], FX[s2]), f2(rdxy.x), mul2(sub2(FYR[s2], FY[s2]), f2(rdxy.y)));
                 const float2 hs = fma2(sub2(div, src), f2(-dt2), ho);
-                DRY[s2] = ACT[s2] & lt2(hs, th);
+                DRY[s2] = ACT[s2] & mask2(lt2(hs, th));
             }
             /* ---- final depth of row L-3 ---- */
             const int r = L - 3;
-            if (r >= rs && r < re) {
-                const int dc = DRY[s3], dN = DRY[s0], dS = DRY[s2];
-                float2 fN = FX[s3], fS = FX[s2], fW = FY[s3], fE = FYR[s3];
-                if (__any_sync(0xffffffffu, (dc | dN | dS) != 0)) {
-                    /* treat_error (SW2D-EFDC.cu:695-725): no outflow from a dry cell */
-                    const int dW = leftbits(dc), dE = rightbits(dc);
-                    const int zN = (gt2(fN, 0.f) & dN) | (lt2(fN, 0.f) & dc);
-                    const int zS = (gt2(fS, 0.f) & dc) | (lt2(fS, 0.f) & dS);
-                    const int zW = (gt2(fW, 0.f) & dW) | (lt2(fW, 0.f) & dc);
-                    const int zE = (gt2(fE, 0.f) & dc) | (lt2(fE, 0.f) & dE);
-                    fN = sel2(zN, f2(0.f), fN);
-                    fS = sel2(zS, f2(0.f), fS);
-                    fW = sel2(zW, f2(0.f), fW);
-                    fE = sel2(zE, f2(0.f), fE);
-                }
+            /* continuity at t+dt, Kahan-compensated, and write-back of the
+             * cell with its north and west faces */
+            auto finish = [&](float2 fN, float2 fS, float2 fW, float2 fE) {
                 const float2 ho = H[s3];
-                const int act = ACT[s3];
-                const int lake = gt2(ho, ewl);
-                float2 src = sel2(lake, f2(rl2), f2(rd2));
-                const float2 wgt = has_rw ? *reinterpret_cast<const float2*>(srw + j * BW + sc) : f2(1.f);
-                if (has_rw) src = mul2(src, wgt);
-                src = sub2(src, sel2(lake, f2(ev2), f2(0.f)));
+                const B2 act = bits2(ACT[s3]);
+                B2 lake = {false, false};
+                float2 src = f2(rd2);
+                if (LAKE) {
+                    lake = gt2(ho, ewl);
+                    src = sel2(lake, f2(rl2), src);
+                }
+                const float2 wgt = RW ? *reinterpret_cast<const float2*>(srw + j * BW + sc) : f2(1.f);
+                if (RW) src = mul2(src, wgt);
+                if (LAKE) src = sub2(src, sel2(lake, f2(ev2), f2(0.f)));
                 const float2 div = fma2(sub2(fS, fN), f2(rdxy.x), mul2(sub2(fE, fW), f2(rdxy.y)));
                 const float2 dh = mul2(sub2(div, src), f2(-dt2));
                 /* Kahan: the increment is small against the depth */
@@ -495,20 +507,24 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 const float2 y = sub2(dh, kc0);
                 const float2 t = add2(ho, y);
                 float2 kc = sub2(sub2(t, ho), y);
-                const int pos = ge2(t, 0.f);
-                const int oa = ownm & act;
+                const B2 pos = ge2(t, 0.f);
+                const B2 oa = bits2(ownm) & act;
                 {
-                    const int neg = oa & ~pos;
-                    clamp -= ((neg & 1) ? t.x : 0.f) + ((neg & 2) ? t.y : 0.f);
+                    const float2 ng = sel2(andnot(oa, pos), t, f2(0.f));
+                    clamp -= ng.x + ng.y;
                 }
-                if (P.ledger_cells) {
+                if (LAKE) {
                     float2 pw = sel2(lake, f2(P.pct_lake), f2(P.pct_land));
-                    if (has_rw) pw = mul2(pw, wgt);
-                    rainacc += ((oa & 1) ? pw.x : 0.f) + ((oa & 2) ? pw.y : 0.f);
-                    const int ol = oa & lake;
-                    evc += (float)((ol & 1) + (ol >> 1));
+                    if (RW) pw = mul2(pw, wgt);
+                    pw = sel2(oa, pw, f2(0.f));
+                    rainacc += pw.x + pw.y;
+                    const float2 ec = sel2(oa & lake, f2(1.f), f2(0.f));
+                    evc += ec.x + ec.y;
                 }
-                if (r == R - 1) qout += ((oa & 1) ? fS.x : 0.f) + ((oa & 2) ? fS.y : 0.f);
+                if (r == R - 1) {
+                    const float2 qo = sel2(oa, fS, f2(0.f));
+                    qout += qo.x + qo.y;
+                }
                 kc = sel2(act & pos, kc, f2(0.f));
                 const float2 hout = sel2(act, make_float2(fmaxf(t.x, 0.f), fmaxf(t.y, 0.f)), f2(0.f));
                 const size_t g = (size_t)(r + M_H) * Pp + (cg + M_H);
@@ -524,6 +540,24 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                     P.qx[nxt][g] = fN.x;
                     P.qy[nxt][g] = fW.x;
                     if (r == R - 1) P.qx[nxt][g + Pp] = fS.x;
+                }
+            };
+            if (r >= rs && r < re) {
+                const int dc = DRY[s3], dN = DRY[s0], dS = DRY[s2];
+                if (__any_sync(0xffffffffu, (dc | dN | dS) != 0)) {
+                    /* treat_error (SW2D-EFDC.cu:695-725): no outflow from a dry
+                     * cell.  The whole finish is repeated in both branches so
+                     * that the rare clipping stays a real branch. */
+                    const int dW = leftbits(dc), dE = rightbits(dc);
+                    const B2 bc = bits2(dc), bN = bits2(dN), bS = bits2(dS), bW = bits2(dW), bE = bits2(dE);
+                    const float2 fN = FX[s3], fS = FX[s2], fW = FY[s3], fE = FYR[s3];
+                    const B2 zN = (gt2(fN, 0.f) & bN) | (lt2(fN, 0.f) & bc);
+                    const B2 zS = (gt2(fS, 0.f) & bc) | (lt2(fS, 0.f) & bS);
+                    const B2 zW = (gt2(fW, 0.f) & bW) | (lt2(fW, 0.f) & bc);
+                    const B2 zE = (gt2(fE, 0.f) & bc) | (lt2(fE, 0.f) & bE);
+                    finish(sel2(zN, f2(0.f), fN), sel2(zS, f2(0.f), fS), sel2(zW, f2(0.f), fW), sel2(zE, f2(0.f), fE));
+                } else {
+                    finish(FX[s3], FX[s2], FY[s3], FYR[s3]);
                 }
             }
         }
@@ -730,14 +764,32 @@ __global__ void k32_volume(const Scn32* __restrict__ scns, int iscn, double* out
     }
 }
 
-int fp32_configure_kernels() {
-    cudaError_t e = cudaFuncSetAttribute(k32_march, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fp32_smem_bytes());
-    return e == cudaSuccess ? 0 : -1;
+typedef void (*MarchFn)(const Scn32*, const int4*, Part32*);
+static const MarchFn kMarch[T32_NCLASS] = {
+    k32_march<false, false, false>, k32_march<true, false, false>, k32_march<false, true, false>,
+    k32_march<true, true, false>,   k32_march<false, false, true>,  k32_march<true, false, true>,
+    k32_march<false, true, true>,   k32_march<true, true, true>,
+};
+
+int fp32_feature_class(const Scn32& d) {
+    return (d.cls ? 1 : 0) | (d.rainw ? 2 : 0) | (d.ledger_cells ? 4 : 0);
 }
 
-void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, int nwork, Part32* d_part,
-                           cudaStream_t s) {
-    if (nwork > 0) k32_march<<<nwork, NT, fp32_smem_bytes(), s>>>(d_scn, d_work, d_part);
+int fp32_configure_kernels() {
+    for (int k = 0; k < T32_NCLASS; k++) {
+        cudaError_t e = cudaFuncSetAttribute(kMarch[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)fp32_smem_bytes());
+        if (e != cudaSuccess) return -1;
+    }
+    return 0;
+}
+
+void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, const int* class_first,
+                           const int* class_n, Part32* d_part, cudaStream_t s) {
+    for (int k = 0; k < T32_NCLASS; k++)
+        if (class_n[k] > 0)
+            kMarch[k]<<<class_n[k], NT, fp32_smem_bytes(), s>>>(d_scn, d_work + class_first[k],
+                                                                d_part + class_first[k]);
     k32_finalize<<<(nscn + 3) / 4, 128, 0, s>>>(d_scn, nscn, d_part);
 }
 

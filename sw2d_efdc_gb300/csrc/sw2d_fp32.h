@@ -94,8 +94,13 @@ struct Scn32 {
     float ntab[T32_MAXCLASS];
 };
 
-void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, int nwork, Part32* d_part,
-                           cudaStream_t s);
+/* Feature class of a scenario (bit 0 class raster, bit 1 rain-weight field,
+ * bit 2 lake fraction): the marching kernel is specialised per class and
+ * the work list holds each class's items contiguously. */
+constexpr int T32_NCLASS = 8;
+int fp32_feature_class(const Scn32& d);
+void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, const int* class_first,
+                           const int* class_n, Part32* d_part, cudaStream_t s);
 void fp32_launch_prime(const Scn32* d_scn, int nscn, cudaStream_t s);
 void fp32_launch_volume(const Scn32* d_scn, int iscn, const Scn32& host_scn, double* d_out, cudaStream_t s);
 size_t fp32_smem_bytes();
