@@ -77,7 +77,7 @@ int Engine32::init(std::string* err) {
     ECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     ECK(cudaEventCreate(&ev_a_));
     ECK(cudaEventCreate(&ev_b_));
-    ECK(cudaMalloc(&d_tmp_, 4 * sizeof(double)));
+    ECK(cudaMalloc(&d_tmp_, fp32_volume_scratch_bytes()));
     if (fp32_configure_kernels() != 0) {
         if (err) *err = "cannot enable the FP32 kernel's shared memory";
         return SW2D_ERR_CUDA;
@@ -101,6 +101,60 @@ size_t Engine32::scenario_bytes(int rows, int cols, bool rain_field, int outlet_
     const size_t tiles = (size_t)((cols + M_CW - 1) / M_CW) * ((rows + 15) / 16);
     b += tiles * sizeof(float) + (size_t)outlet_cap * 16 + sizeof(Clock32) + 4096;
     return b;
+}
+
+int Engine32::segment_rows_for(int rows, int cols) {
+    if (seg_rows_ > 0) return seg_rows_;
+    if (tuning_ || (long long)rows * cols < (1ll << 20)) return 128;
+    auto bucket = [](int n) {
+        int b = 0;
+        while ((1 << b) < n) b++;
+        return b;
+    };
+    const std::pair<int, int> key(bucket(rows), bucket(cols));
+    auto it = seg_cache_.find(key);
+    if (it != seg_cache_.end()) return it->second;
+    /* time the candidates on a scratch scenario of the bucket's size: a wet
+     * 1% plane with gentle bumps, CFL steps; skipped (128) when the device
+     * has no room for it */
+    const int tr = 1 << key.first, tc = 1 << key.second;
+    int best = 128;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > 3 * scenario_bytes(tr, tc, false, 0)) {
+        std::vector<double> dem((size_t)tr * tc), depth((size_t)tr * tc, 0.05);
+        for (int r = 0; r < tr; r++)
+            for (int c = 0; c < tc; c++)
+                dem[(size_t)r * tc + c] = 0.01 * (tr - 1 - r) + 0.05 * std::sin(0.05 * c) * std::cos(0.03 * r);
+        const double rain0 = 0.0;
+        ScenarioInput in;
+        in.rows = tr;
+        in.cols = tc;
+        in.dem = dem.data();
+        in.depth = depth.data();
+        in.rain = &rain0;
+        in.nrain = 1;
+        in.t_end = 1e9;
+        double best_ms = 1e300;
+        for (int cand : {64, 128, 256, 512}) {
+            if (cand > 2 * tr) continue;
+            Engine32 scratch(device_);
+            std::string e2;
+            scratch.tuning_ = true;
+            scratch.seg_rows_ = cand;
+            int idx = -1;
+            if (scratch.init(&e2) || scratch.add(in, 0, &e2, &idx) || scratch.set_t_end(-1, 1e9, &e2) ||
+                scratch.run(4, &e2) || scratch.run(8, &e2))
+                break;
+            const double ms = scratch.last_ms();
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = cand;
+            }
+        }
+        cudaSetDevice(device_);
+    }
+    seg_cache_[key] = best;
+    return best;
 }
 
 size_t Engine32::bytes_in_use() const {
@@ -128,7 +182,7 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     S.P = P;
     S.NR = NR;
     const size_t cells = (size_t)P * NR;
-    const int seg = seg_rows_ > 0 ? seg_rows_ : 128;
+    const int seg = segment_rows_for(R, C);
     const int tx = (C + M_CW - 1) / M_CW, ty = (R + seg - 1) / seg;
     auto alloc = [&](size_t bytes, void** p) -> int {
         cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));

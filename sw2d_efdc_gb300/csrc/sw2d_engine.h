@@ -7,6 +7,7 @@
 #include "sw2d.h"
 #include "sw2d_fp32.h"
 
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -67,8 +68,13 @@ class Engine32 {
     long long last_iters() const { return last_iters_; }
     int nwork() const { return (int)work_.size(); }
     int sync(std::string* err);
-    /* rows per work item of scenarios added from now on (0 = default 128) */
+    /* rows per work item of scenarios added from now on (0 = chosen by
+     * segment_rows_for) */
     void set_segment_rows(int rows) { seg_rows_ = rows; }
+    /* Rows per work item for a raster of this size: the fixed value when one
+     * is set, else the autotuned choice (timed once per power-of-two size
+     * bucket on a scratch scenario) for rasters of >= 1 Mcell, else 128. */
+    int segment_rows_for(int rows, int cols);
 
   private:
     int rebuild(std::string* err);
@@ -92,6 +98,8 @@ class Engine32 {
     double last_ms_ = 0.0;
     long long last_iters_ = 0;
     int seg_rows_ = 0;
+    bool tuning_ = false;                       /* a scratch engine of the autotuner */
+    std::map<std::pair<int, int>, int> seg_cache_; /* size bucket -> tuned rows per work item */
 };
 
 } // namespace sw2d

@@ -31,6 +31,8 @@
 #include <math.h>
 #include <stddef.h>
 
+#include <algorithm>
+
 namespace sw2d {
 
 #define NW M_NW
@@ -721,48 +723,88 @@ __global__ void k32_prime(const Scn32* __restrict__ scns, int nscn) {
 /* volume = sum of (h - kc) over active cells, and the CFL face speed of the
  * current state (the rule of k32_step), for one scenario (one block, fixed
  * order) */
-__global__ void k32_volume(const Scn32* __restrict__ scns, int iscn, double* out) {
+/* Volume (depth minus its Kahan compensation, over active cells) and the
+ * CFL face-speed sum of a scenario's current state: rows spread over up to
+ * kVolBlocks blocks (columns over the threads, coalesced), partials reduced
+ * in a fixed order by one block. */
+constexpr int kVolBlocks = 1024;
+struct VolPart {
+    double vol;
+    float sx, sy;
+};
+
+__device__ __forceinline__ void block_reduce_vol(double& vol, float& sx, float& sy) {
+    __shared__ double sv[32];
+    __shared__ float smx[32], smy[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        vol += __shfl_xor_sync(0xffffffffu, vol, o);
+        sx = fmaxf(sx, __shfl_xor_sync(0xffffffffu, sx, o));
+        sy = fmaxf(sy, __shfl_xor_sync(0xffffffffu, sy, o));
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) {
+        sv[w] = vol;
+        smx[w] = sx;
+        smy[w] = sy;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < nw; k++) {
+            vol += sv[k];
+            sx = fmaxf(sx, smx[k]);
+            sy = fmaxf(sy, smy[k]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k32_volume_part(const Scn32* __restrict__ scns, int iscn,
+                                                       VolPart* __restrict__ part) {
     const Scn32& P = scns[iscn];
     const int cur = P.clk->slot.cur;
     const float th = P.th;
     double vol = 0.0;
     float sx = 0.f, sy = 0.f;
-    for (long long k = threadIdx.x; k < (long long)P.R * P.C; k += blockDim.x) {
-        const int r = (int)(k / P.C), c = (int)(k % P.C);
-        const size_t g = (size_t)(r + M_H) * P.P + (c + M_H);
-        if (!is_act(P.z[g])) continue;
-        const float hh = P.h[cur][g];
-        vol += (double)hh - (double)P.kc[g];
-        if (r > 0 && is_act(P.z[g - P.P])) {
-            const float hm = 0.5f * (hh + P.h[cur][g - P.P]);
-            const float q = P.qx[cur][g];
-            if (hm >= th) sx = fmaxf(sx, (fabsf(q != 0.f ? q / hm : 0.f) + fsqrt(P.g * hm)) * P.rdx);
-        }
-        if (c > 0 && is_act(P.z[g - 1])) {
-            const float hn = 0.5f * (hh + P.h[cur][g - 1]);
-            const float q = P.qy[cur][g];
-            if (hn >= th) sy = fmaxf(sy, (fabsf(q != 0.f ? q / hn : 0.f) + fsqrt(P.g * hn)) * P.rdy);
+    for (int r = blockIdx.x; r < P.R; r += gridDim.x) {
+        for (int c = threadIdx.x; c < P.C; c += blockDim.x) {
+            const size_t g = (size_t)(r + M_H) * P.P + (c + M_H);
+            if (!is_act(P.z[g])) continue;
+            const float hh = P.h[cur][g];
+            vol += (double)hh - (double)P.kc[g];
+            if (r > 0 && is_act(P.z[g - P.P])) {
+                const float hm = 0.5f * (hh + P.h[cur][g - P.P]);
+                const float q = P.qx[cur][g];
+                if (hm >= th) sx = fmaxf(sx, (fabsf(q != 0.f ? q / hm : 0.f) + fsqrt(P.g * hm)) * P.rdx);
+            }
+            if (c > 0 && is_act(P.z[g - 1])) {
+                const float hn = 0.5f * (hh + P.h[cur][g - 1]);
+                const float q = P.qy[cur][g];
+                if (hn >= th) sy = fmaxf(sy, (fabsf(q != 0.f ? q / hn : 0.f) + fsqrt(P.g * hn)) * P.rdy);
+            }
         }
     }
-    __shared__ double sv[1024];
-    __shared__ float smx[1024], smy[1024];
-    sv[threadIdx.x] = vol;
-    smx[threadIdx.x] = sx;
-    smy[threadIdx.x] = sy;
-    __syncthreads();
-    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) {
-            sv[threadIdx.x] += sv[threadIdx.x + o];
-            smx[threadIdx.x] = fmaxf(smx[threadIdx.x], smx[threadIdx.x + o]);
-            smy[threadIdx.x] = fmaxf(smy[threadIdx.x], smy[threadIdx.x + o]);
-        }
-        __syncthreads();
+    block_reduce_vol(vol, sx, sy);
+    if (threadIdx.x == 0) part[blockIdx.x] = VolPart{vol, sx, sy};
+}
+
+__global__ void __launch_bounds__(1024) k32_volume_fin(const Scn32* __restrict__ scns, int iscn,
+                                                       const VolPart* __restrict__ part, int n, double* out) {
+    const Scn32& P = scns[iscn];
+    double vol = 0.0;
+    float sx = 0.f, sy = 0.f;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        vol += part[k].vol;
+        sx = fmaxf(sx, part[k].sx);
+        sy = fmaxf(sy, part[k].sy);
     }
+    block_reduce_vol(vol, sx, sy);
     if (threadIdx.x == 0) {
-        out[0] = sv[0] * P.area;
-        out[1] = (double)smx[0] + (double)smy[0];
+        out[0] = vol * P.area;
+        out[1] = (double)sx + (double)sy;
     }
 }
+
+size_t fp32_volume_scratch_bytes() { return 32 + kVolBlocks * sizeof(VolPart); }
 
 typedef void (*MarchFn)(const Scn32*, const int4*, Part32*);
 static const MarchFn kMarch[T32_NCLASS] = {
@@ -798,8 +840,10 @@ void fp32_launch_prime(const Scn32* d_scn, int nscn, cudaStream_t s) {
 }
 
 void fp32_launch_volume(const Scn32* d_scn, int iscn, const Scn32& host_scn, double* d_out, cudaStream_t s) {
-    (void)host_scn;
-    k32_volume<<<1, 1024, 0, s>>>(d_scn, iscn, d_out);
+    const int nb = std::max(1, std::min(host_scn.R, kVolBlocks));
+    VolPart* part = reinterpret_cast<VolPart*>(reinterpret_cast<char*>(d_out) + 32);
+    k32_volume_part<<<nb, 256, 0, s>>>(d_scn, iscn, part);
+    k32_volume_fin<<<1, 1024, 0, s>>>(d_scn, iscn, part, nb, d_out);
 }
 
 } // namespace sw2d

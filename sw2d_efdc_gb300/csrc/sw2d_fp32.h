@@ -102,7 +102,10 @@ int fp32_feature_class(const Scn32& d);
 void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, const int* class_first,
                            const int* class_n, Part32* d_part, cudaStream_t s);
 void fp32_launch_prime(const Scn32* d_scn, int nscn, cudaStream_t s);
+/* volume and CFL speed of one scenario into d_out[0..1]; d_out holds
+ * fp32_volume_scratch_bytes() (the partials follow the two results) */
 void fp32_launch_volume(const Scn32* d_scn, int iscn, const Scn32& host_scn, double* d_out, cudaStream_t s);
+size_t fp32_volume_scratch_bytes();
 size_t fp32_smem_bytes();
 int fp32_configure_kernels();
 

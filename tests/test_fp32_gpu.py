@@ -90,3 +90,17 @@ def test_fp32_oracle_volume_and_outlet():
     assert len(t32) == n
     assert np.abs(np.interp(to, t32, q32) - qo).max() < 1e-3 * max(qo.max(), 1e-9) + 1e-6
     assert m32.ledger()["volume"] == pytest.approx(o.ledger()["volume"], rel=1e-4)
+
+
+def test_fp32_work_item_rows_change_results_only_by_rounding(monkeypatch):
+    # the autotuner picks the rows per work item; the tile datum follows the
+    # work items, so results may differ by binary32 rounding of the bed only
+    case = bumpy_case(R=300, C=260, seed=25, t_end=40.0, dt=0.05, holes=False)
+    depths = []
+    for rows in ("64", "256"):
+        monkeypatch.setenv("SW2D_SEGMENT_ROWS", rows)
+        m = model_from_case(case, precision=api.FP32)
+        m.advance(case.t_end)
+        depths.append(m.depth())
+        m.close()
+    assert np.abs(depths[0] - depths[1]).max() < 1e-5

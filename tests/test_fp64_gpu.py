@@ -32,6 +32,15 @@ def _assert_same(g, o, keys=("h", "qx", "qy", "uu", "vv", "uua", "vva")):
         assert not bad.any(), "%s differs at %d cells, max %.3e" % (k, bad.sum(), np.nanmax(np.abs(a - b)))
 
 
+def _wet_dry_ties(h, h_ref, th):
+    """Cells whose wet/dry state (h > th) differs from the reference flavour's;
+    all of them must be threshold ties (|h_ref - th| <= 1e-9 m).  Returns the
+    tie count, which the tests report."""
+    differ = (h > th) != (h_ref > th)
+    assert np.all(np.abs(h_ref[differ] - th) <= DH_TOL), "wet/dry mask differs away from the threshold"
+    return int(differ.sum())
+
+
 def _run_pair(case, iters=None):
     m = model_from_case(case)
     od = O.Oracle(case, math=O.MATH_DEVICE)
@@ -57,6 +66,7 @@ def test_fixed_dt_reference_series_bitwise():
     g = _fields(m)
     _assert_same(g, od.fields())
     assert np.abs(g["h"] - ol.fields()["h"]).max() <= DH_TOL
+    print("wet/dry threshold ties:", _wet_dry_ties(g["h"], ol.fields()["h"], case.th))
 
 
 def test_cfl_outflow_fields_bitwise():
@@ -71,6 +81,7 @@ def test_cfl_outflow_fields_bitwise():
     g = _fields(m)
     _assert_same(g, od.fields())
     assert np.abs(g["h"] - ol.fields()["h"]).max() <= DH_TOL
+    print("wet/dry threshold ties:", _wet_dry_ties(g["h"], ol.fields()["h"], case.th))
     lg, lo = m.ledger(), od.ledger()
     for k in ("volume", "rain_in", "outflow", "clamp_gain"):
         assert lg[k] == pytest.approx(lo[k], rel=1e-12, abs=1e-12), k
