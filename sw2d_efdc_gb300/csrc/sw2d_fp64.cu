@@ -123,140 +123,92 @@ __device__ void prepare_slot(const StepParams& p, Slot* s, double t, double smax
 
 __device__ __forceinline__ double face_manning(const StepParams& p, size_t a, size_t b) {
     if (!p.mcls) return p.manning;
-    return 0.50 * (p.mtab[p.mcls[a]] + p.mtab[p.mcls[b]]);
+    return sw2d_half(p.mtab[p.mcls[a]] + p.mtab[p.mcls[b]]);
 }
 
 __device__ __forceinline__ double friction(const StepParams& p, double nf, double sq, double hm) {
     /* :193-198; the division by pow(hm, 1.333333) as a product with hm^-1.333333 */
-    if (hm <= p.th) return 0.00;
+    if (sw2d_le_pos(hm, p.th)) return 0.00;
     return (p.g * nf * nf * sq) * sw2d_rpow_manning(hm);
 }
 
-/* x face between cell w = (r-1, c) and e = (r, c), positive southward */
-__device__ __forceinline__ double flux_x(const StepParams& p, const double* __restrict__ h,
-                                         const double* __restrict__ umo, int r, int c, size_t e,
-                                         double dt2, double dt2dx, double dt2dy) {
-    const double th = p.th, gg = p.g;
-    const int P = p.P;
-    const size_t w = e - P;
-    const double* __restrict__ z = p.z;
-    const double* __restrict__ uu1 = p.uu1;
-    const double* __restrict__ vv1 = p.vv1;
-    const uint8_t fe = p.flags[e], fw = p.flags[w];
-    const double he = h[e], hw = h[w];
-    if (r == p.R && p.outflow_south) {
-        if ((fw & SW2D_F_ACTIVE) && hw > th) return 0.5440 * hw * sqrt(gg * hw);
-        return 0;
-    }
-    if (!(fe & SW2D_F_ACTIVE) || !(fw & SW2D_F_ACTIVE)) return 0;
-    if (!((hw > th) || (he > th))) return 0;
-    const double ze = z[e], zw = z[w];
-    const double hhe = he + ze;
-    const double hhw = hw + zw;
-    const double hhep = he - th;
-    const double hhwp = hw - th;
-    if (hhe < zw) {
-        if (hw > th) return 0.5440 * hw * sqrt(gg * hw);
-        return 0;
-    } else if (hhw < ze) {
-        if (he > th) return -0.544 * he * sqrt(gg * he);
-        return 0;
-    } else if (hhep * hhwp < 0) {
-        if ((he > 0) || (hw > 0)) {
-            double hhan = hhep - hhwp;
-            double sgnm = copysign(1.0, hhan);
-            double hh3 = fmax(hhe, hhw) - fmax(ze, zw);
-            return -sgnm * 0.350 * hh3 * sqrt(2.00 * gg * hh3);
-        }
-        return 0;
-    }
-    const double hm = 0.50 * (he + hw);
-    const double u13 = gg * hm * dt2dx * (hhe - hw - zw);
-    const double uc = uu1[e];
-    const double u11uur = 0.50 * (uu1[e + P] + uc);
-    const double u11uul = 0.50 * (uc + uu1[w]);
-    const double um0 = umo[e], umS = umo[e + P], umN = umo[w];
-    const double umr = u11uur * (umS + um0) * 0.50 + fabs(u11uur) * (um0 - umS) * 0.50;
-    const double uml = u11uul * (um0 + umN) * 0.50 + fabs(u11uul) * (umN - um0) * 0.50;
-    const double u11 = dt2dx * (umr - uml);
-    const double v_e = vv1[e], v_e1 = vv1[e + 1], v_w = vv1[w], v_w1 = vv1[w + 1];
-    double u12;
-    if (c == 0) {
-        u12 = 0;
-    } else {
-        const double u12vvu = 0.50 * (v_e1 + v_w1);
-        const double u12vvd = 0.50 * (v_e + v_w);
-        const double umE = umo[e + 1], umW = umo[e - 1];
-        const double umu = u12vvu * (umE + um0) * 0.50 + fabs(u12vvu) * (um0 - umE) * 0.50;
-        const double umd = u12vvd * (umW + um0) * 0.50 + fabs(u12vvd) * (umW - um0) * 0.50;
-        u12 = dt2dy * (umu - umd);
-    }
-    const double vva = 0.250 * (v_e + v_e1 + v_w + v_w1);
-    const double sqx = sqrt(uc * uc + vva * vva);
-    const double ram = friction(p, face_manning(p, e, w), sqx, hm);
-    return ((1.00 - dt2 * ram * 0.50) * um0 + (-u11 - u12 - u13)) / (1.00 + dt2 * ram * 0.50);
+/* Upwind donor-cell transport across the edge between two neighbouring
+ * faces of the same orientation (the reference's umr/uml, umu/umd, vnr/vnl,
+ * vnu/vnd, SW2D-EFDC.cu:171-189, :288-306):
+ *     a (q1 + q0) / 2 + |a| (q0 - q1) / 2,   a = (w1 + w0) / 2,
+ * with q0 the discharge of the face the edge is read from first.  The
+ * reference evaluates every edge twice, once from each face beside it, with
+ * the same operands in the same order (+ commutes exactly), so one
+ * evaluation per edge gives bit-identical fluxes. */
+__device__ __forceinline__ double edge_term(double w1, double w0, double q0, double q1) {
+    const double a = sw2d_half(w1 + w0);
+    return sw2d_half(a * (q1 + q0)) + sw2d_half(fabs(a) * (q0 - q1));
 }
 
-/* y face between cell s = (r, c-1) and n = (r, c), positive eastward */
-__device__ __forceinline__ double flux_y(const StepParams& p, const double* __restrict__ h,
-                                         const double* __restrict__ vno, int r, int c, size_t n,
-                                         double dt2, double dt2dx, double dt2dy) {
-    const double th = p.th, gg = p.g;
-    const int P = p.P;
-    const size_t so = n - 1;
-    const double* __restrict__ z = p.z;
-    const double* __restrict__ uu1 = p.uu1;
-    const double* __restrict__ vv1 = p.vv1;
-    const uint8_t fn = p.flags[n], fs = p.flags[so];
-    if (!(fn & SW2D_F_ACTIVE) || !(fs & SW2D_F_ACTIVE)) return 0;
-    const double hn = h[n], hs = h[so];
-    if (!((hs > th) || (hn > th))) return 0;
-    const double zn = z[n], zs = z[so];
-    const double hhn = hn + zn;
-    const double hhs = hs + zs;
-    const double hhnp = hn - th;
-    const double hhsp = hs - th;
-    if (hhn < zs) {
-        if (hs > th) return 0.5440 * hs * sqrt(gg * hs);
-        return 0;
-    } else if (hhs < zn) {
-        if (hn > th) return -0.544 * hn * sqrt(gg * hn);
-        return 0;
-    } else if (hhnp * hhsp < 0) {
-        if ((hn > 0) || (hs > 0)) {
-            double hhan = hhnp - hhsp;
-            double sgnm = copysign(1.0, hhan);
-            double hh3 = fmax(hhn, hhs) - fmax(zn, zs);
+/* Kind of a face (SW2D-EFDC.cu:115-165, same tests in the same order):
+ *   0 closed (an inactive side, or both sides at or below th)
+ *   1 momentum (gravity, convection, friction)
+ *   2 weir from side a, 3 weir from side b (a side's surface below the
+ *     other side's bed), 4 dry-bed front (exactly one side above th).
+ * Side a is the north (x faces) / west (y faces) cell.  The product
+ * (hb - th) (ha - th) < 0 of the reference is decided from the two
+ * comparisons with th (the differences keep the comparisons' signs and
+ * their product of depths cannot underflow). */
+struct FaceK {
+    int kind;
+    bool wa, wb;
+    double ha, hb, za, zb, hha, hhb;
+};
+__device__ __forceinline__ FaceK classify(bool act, double ha, double hb, const double* __restrict__ z, size_t ia,
+                                          size_t ib, double th) {
+    FaceK f;
+    f.kind = 0;
+    f.ha = ha;
+    f.hb = hb;
+    f.wa = sw2d_gt_pos(ha, th);
+    f.wb = sw2d_gt_pos(hb, th);
+    f.za = f.zb = f.hha = f.hhb = 0.0;
+    if (!act || !(f.wa || f.wb)) return f;
+    f.za = z[ia];
+    f.zb = z[ib];
+    f.hhb = hb + f.zb;
+    f.hha = ha + f.za;
+    if (sw2d_lt(f.hhb, f.za)) f.kind = 2;
+    else if (sw2d_lt(f.hha, f.zb)) f.kind = 3;
+    else if ((f.wb && sw2d_lt_pos(ha, th)) || (f.wa && sw2d_lt_pos(hb, th))) f.kind = 4;
+    else f.kind = 1;
+    return f;
+}
+
+/* discharge of a non-momentum face */
+__device__ __forceinline__ double face_special(const FaceK& f, double th, double gg) {
+    switch (f.kind) {
+    case 2: return f.wa ? 0.5440 * f.ha * sqrt(gg * f.ha) : 0.0;
+    case 3: return f.wb ? -0.544 * f.hb * sqrt(gg * f.hb) : 0.0;
+    case 4:
+        if (sw2d_gt0(f.hb) || sw2d_gt0(f.ha)) {
+            const double hhan = (f.hb - th) - (f.ha - th);
+            const double sgnm = copysign(1.0, hhan);
+            const double hh3 = fmax(f.hhb, f.hha) - fmax(f.zb, f.za);
             return -sgnm * 0.350 * hh3 * sqrt(2.00 * gg * hh3);
         }
-        return 0;
+        return 0.0;
+    default: return 0.0;
     }
-    const double hnf = 0.50 * (hn + hs);
-    const double v13 = gg * hnf * dt2dy * (hhn - hs - zs);
-    const double vn0 = vno[n];
-    const double ua = uu1[n], ub = uu1[n + P], uc = uu1[n - 1], ud = uu1[n + P - 1];
-    double v11;
-    if (r == 0) {
-        v11 = 0;
-    } else {
-        const double v11uur = 0.50 * (ub + ud);
-        const double v11uul = 0.50 * (ua + uc);
-        const double vS = vno[n + P], vN = vno[n - P];
-        const double vnr = v11uur * (vS + vn0) * 0.50 + fabs(v11uur) * (vn0 - vS) * 0.50;
-        const double vnl = v11uul * (vn0 + vN) * 0.50 + fabs(v11uul) * (vN - vn0) * 0.50;
-        v11 = dt2dx * (vnr - vnl);
-    }
-    const double vc = vv1[n];
-    const double v12vvu = 0.50 * (vv1[n + 1] + vc);
-    const double v12vvd = 0.50 * (vc + vv1[n - 1]);
-    const double vE = vno[n + 1], vW = vno[n - 1];
-    const double vnu = v12vvu * (vE + vn0) * 0.50 + fabs(v12vvu) * (vn0 - vE) * 0.50;
-    const double vnd = v12vvd * (vW + vn0) * 0.50 + fabs(v12vvd) * (vW - vn0) * 0.50;
-    const double v12 = dt2dy * (vnu - vnd);
-    const double uua = 0.250 * (ua + ub + uc + ud);
-    const double sqy = sqrt(uua * uua + vc * vc);
-    const double ram = friction(p, face_manning(p, n, so), sqy, hnf);
-    return ((1.00 - dt2 * ram * 0.50) * vn0 + (-v11 - v12 - v13)) / (1.00 + dt2 * ram * 0.50);
+}
+
+/* momentum update of a face (SW2D-EFDC.cu:165-202 x, :282-319 y): along /
+ * across are the face's two edge differences, already scaled. */
+__device__ __forceinline__ double face_momentum(const StepParams& p, const FaceK& f, double q0, double u0,
+                                                double vt, double along, double across, double dt2,
+                                                double dt2n, size_t ia, size_t ib) {
+    const double gg = p.g;
+    const double hm = sw2d_half(f.hb + f.ha);
+    const double g13 = gg * hm * dt2n * (f.hhb - f.ha - f.za);
+    const double sq = sqrt(u0 * u0 + vt * vt);
+    const double ram = friction(p, face_manning(p, ib, ia), sq, hm);
+    const double a = sw2d_half(dt2 * ram);
+    return ((1.00 - a) * q0 + (-along - across - g13)) / (1.00 + a);
 }
 
 __device__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* sm);
@@ -281,36 +233,112 @@ __device__ __forceinline__ unsigned long long block_face_speed_max(bool ok, doub
     return block_max_u64(bits, smu);
 }
 
-__global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_flux(StepParams p, int cur) {
+__global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, int cur) {
     __shared__ float smf[SW2D_BX * SW2D_BY / 32];
     __shared__ unsigned long long smu[SW2D_BX * SW2D_BY / 32];
-    const int c = blockIdx.x * SW2D_BX + threadIdx.x;
-    const int r = blockIdx.y * SW2D_BY + threadIdx.y;
+    /* momentum faces of the block, then the edges of the block's cells and of
+     * the row above / column left of it */
+    __shared__ unsigned char regx[SW2D_BY][SW2D_BX], regy[SW2D_BY][SW2D_BX];
+    __shared__ double sea[SW2D_BY + 1][SW2D_BX], sec[SW2D_BY + 1][SW2D_BX];
+    __shared__ double seb[SW2D_BY][SW2D_BX + 1], sed[SW2D_BY][SW2D_BX + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int c = blockIdx.x * SW2D_BX + tx;
+    const int r = blockIdx.y * SW2D_BY + ty;
     const int nxt = cur ^ 1;
     const Slot& s = p.clk->slot[cur];
+    const bool in = (r <= p.R && c <= p.C);
+    const int P = p.P;
+    const size_t i = (size_t)(r + H) * P + (c + H);
+    const double* __restrict__ h = p.h[cur];
+    const double* __restrict__ umo = p.qx[cur];
+    const double* __restrict__ vno = p.qy[cur];
+    const double* __restrict__ uu1 = p.uu1;
+    const double* __restrict__ vv1 = p.vv1;
+    const double th = p.th;
+    /* 1: classify the thread's x face (north of the cell) and y face (west) */
+    FaceK fx, fy;
+    fx.kind = fy.kind = 0;
+    const bool doX = in && s.active && c < p.C, doY = in && s.active && r < p.R;
+    const bool edgeS = doX && r == p.R && p.outflow_south;
+    if (doX && !edgeS) {
+        const uint8_t fe = p.flags[i], fw = p.flags[i - P];
+        fx = classify((fe & fw & SW2D_F_ACTIVE) != 0, h[i - P], h[i], p.z, i - P, i, th);
+    }
+    if (doY) {
+        const uint8_t fn = p.flags[i], fs = p.flags[i - 1];
+        fy = classify((fn & fs & SW2D_F_ACTIVE) != 0, h[i - 1], h[i], p.z, i - 1, i, th);
+    }
+    regx[ty][tx] = (unsigned char)(fx.kind == 1);
+    regy[ty][tx] = (unsigned char)(fy.kind == 1);
+    __syncthreads();
+    /* 2: each edge once, where a momentum face of the block reads it */
+    {
+        const bool rx = regx[ty][tx], ry = regy[ty][tx];
+        const bool rxS = ty + 1 < SW2D_BY && regx[ty + 1][tx], ryS = ty + 1 < SW2D_BY && regy[ty + 1][tx];
+        const bool rxE = tx + 1 < SW2D_BX && regx[ty][tx + 1], ryE = tx + 1 < SW2D_BX && regy[ty][tx + 1];
+        sea[ty + 1][tx] = (rx || rxS) ? edge_term(uu1[i + P], uu1[i], umo[i], umo[i + P]) : 0.0;
+        seb[ty][tx + 1] = (rx || rxE) ? edge_term(vv1[i + 1], vv1[i - P + 1], umo[i], umo[i + 1]) : 0.0;
+        sec[ty + 1][tx] = (ry || ryS) ? edge_term(uu1[i + P], uu1[i + P - 1], vno[i], vno[i + P]) : 0.0;
+        sed[ty][tx + 1] = (ry || ryE) ? edge_term(vv1[i + 1], vv1[i], vno[i], vno[i + 1]) : 0.0;
+        if (ty == 0) { /* warp 0: the row above, read by the first row's faces */
+            const size_t u = i - P;
+            sea[0][tx] = rx ? edge_term(uu1[u + P], uu1[u], umo[u], umo[u + P]) : 0.0;
+            sec[0][tx] = ry ? edge_term(uu1[u + P], uu1[u + P - 1], vno[u], vno[u + P]) : 0.0;
+        } else if (ty == 1 && tx < SW2D_BY) { /* warp 1, eight lanes: the column left */
+            const size_t l = (size_t)(blockIdx.y * SW2D_BY + tx + H) * P + (blockIdx.x * SW2D_BX - 1 + H);
+            seb[tx][0] = regx[tx][0] ? edge_term(vv1[l + 1], vv1[l - P + 1], umo[l], umo[l + 1]) : 0.0;
+            sed[tx][0] = regy[tx][0] ? edge_term(vv1[l + 1], vv1[l], vno[l], vno[l + 1]) : 0.0;
+        }
+    }
+    __syncthreads();
+    /* 3: face discharges */
     bool okx = false, oky = false;
     double hmx = 0, hmy = 0, vx = 0, vy = 0;
-    if (r <= p.R && c <= p.C) {
-        const size_t i = (size_t)(r + H) * p.P + (c + H);
+    if (in) {
         if (!s.active) {
-            if (c < p.C) p.qx[nxt][i] = p.qx[cur][i];
-            if (r < p.R) p.qy[nxt][i] = p.qy[cur][i];
+            if (c < p.C) p.qx[nxt][i] = umo[i];
+            if (r < p.R) p.qy[nxt][i] = vno[i];
         } else {
-            const double dt2 = s.dt2, dt2dx = s.dt2dx, dt2dy = s.dt2dy;
-            const double* __restrict__ h = p.h[cur];
-            if (c < p.C) p.qx[nxt][i] = flux_x(p, h, p.qx[cur], r, c, i, dt2, dt2dx, dt2dy);
-            if (r < p.R) p.qy[nxt][i] = flux_y(p, h, p.qy[cur], r, c, i, dt2, dt2dx, dt2dy);
+            const double dt2 = s.dt2, dt2dx = s.dt2dx, dt2dy = s.dt2dy, gg = p.g;
+            if (doX) {
+                double F;
+                if (edgeS) { /* south edge: free overfall when open */
+                    const double hw = h[i - P];
+                    F = ((p.flags[i - P] & SW2D_F_ACTIVE) && sw2d_gt_pos(hw, th)) ? 0.5440 * hw * sqrt(gg * hw)
+                                                                                     : 0.0;
+                } else if (fx.kind == 1) {
+                    const double u11 = dt2dx * (sea[ty + 1][tx] - sea[ty][tx]);
+                    const double u12 = (c == 0) ? 0.0 : dt2dy * (seb[ty][tx + 1] - seb[ty][tx]);
+                    const double vt = sw2d_quarter(vv1[i] + vv1[i + 1] + vv1[i - P] + vv1[i - P + 1]);
+                    F = face_momentum(p, fx, umo[i], uu1[i], vt, u11, u12, dt2, dt2dx, i - P, i);
+                } else {
+                    F = face_special(fx, th, gg);
+                }
+                p.qx[nxt][i] = F;
+            }
+            if (doY) {
+                double F;
+                if (fy.kind == 1) {
+                    const double v11 = (r == 0) ? 0.0 : dt2dx * (sec[ty + 1][tx] - sec[ty][tx]);
+                    const double v12 = dt2dy * (sed[ty][tx + 1] - sed[ty][tx]);
+                    const double ut = sw2d_quarter(uu1[i] + uu1[i + P] + uu1[i - 1] + uu1[i + P - 1]);
+                    F = face_momentum(p, fy, vno[i], vv1[i], ut, v11, v12, dt2, dt2dy, i - 1, i);
+                } else {
+                    F = face_special(fy, th, gg);
+                }
+                p.qy[nxt][i] = F;
+            }
             if (p.dt_mode == 1) {
                 const uint8_t fc = p.flags[i];
-                if (c < p.C && r > 0 && r < p.R && (fc & p.flags[i - p.P] & SW2D_F_ACTIVE)) {
-                    hmx = 0.50 * (h[i] + h[i - p.P]);
-                    okx = hmx >= p.th;
-                    vx = p.uu1[i];
+                if (c < p.C && r > 0 && r < p.R && (fc & p.flags[i - P] & SW2D_F_ACTIVE)) {
+                    hmx = sw2d_half(h[i] + h[i - P]);
+                    okx = sw2d_ge_pos(hmx, th);
+                    vx = uu1[i];
                 }
                 if (r < p.R && c > 0 && c < p.C && (fc & p.flags[i - 1] & SW2D_F_ACTIVE)) {
-                    hmy = 0.50 * (h[i] + h[i - 1]);
-                    oky = hmy >= p.th;
-                    vy = p.vv1[i];
+                    hmy = sw2d_half(h[i] + h[i - 1]);
+                    oky = sw2d_ge_pos(hmy, th);
+                    vy = vv1[i];
                 }
             }
         }
@@ -334,7 +362,7 @@ __device__ __forceinline__ double continuity(const StepParams& p, size_t i, uint
                                              double ev, const double* ql, double* raw,
                                              double* rain_term) {
     double pct, evapo;
-    if (ho > p.ev_wl_min) {
+    if (sw2d_gt(ho, p.ev_wl_min)) {
         pct = p.pct_lake;
         evapo = ev;
     } else {
@@ -351,7 +379,7 @@ __device__ __forceinline__ double continuity(const StepParams& p, size_t i, uint
                             rcell * pct + evapo);
     *raw = hn;
     *rain_term = rcell * pct;
-    hn = fmax(hn, 0.00);
+    hn = sw2d_max0(hn);
     if (!(f & SW2D_F_ACTIVE)) hn = 0.00;
     return hn;
 }
@@ -370,7 +398,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_hstar(StepParams p, int
     double raw, rt;
     const double hs = continuity(p, i, f, p.h[cur][i], fx[i + p.P] - fx[i], fy[i + 1] - fy[i], s.dt2,
                                  s.rr1, s.ev1, s.ql1, &raw, &rt);
-    p.drys[i] = (uint8_t)((f & SW2D_F_ACTIVE) && hs < p.th);
+    p.drys[i] = (uint8_t)((f & SW2D_F_ACTIVE) && sw2d_lt_pos(hs, p.th));
 }
 
 /* ------------------------------------------------------------------------ */
@@ -516,7 +544,6 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_depth(StepParams p, int
     const int nxt = cur ^ 1;
     const Slot& s = p.clk->slot[cur];
     double vr = 0.0, ve = 0.0, vq = 0.0;
-    bool wet = false;
     double fN = 0, fS = 0, fW = 0, fE = 0, hn = 0;
     if (r < p.R && c < p.C) {
         const int P = p.P;
@@ -535,22 +562,21 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_depth(StepParams p, int
             fS = fx[i + P];
             fW = fy[i];
             fE = fy[i + 1];
-            if ((fN > 0 && d[i - P]) || (fN < 0 && dc)) fN = 0;
-            if ((fS > 0 && dc) || (fS < 0 && d[i + P])) fS = 0;
-            if ((fW > 0 && d[i - 1]) || (fW < 0 && dc)) fW = 0;
-            if ((fE > 0 && dc) || (fE < 0 && d[i + 1])) fE = 0;
+            if ((sw2d_gt0(fN) && d[i - P]) || (sw2d_lt0(fN) && dc)) fN = 0;
+            if ((sw2d_gt0(fS) && dc) || (sw2d_lt0(fS) && d[i + P])) fS = 0;
+            if ((sw2d_gt0(fW) && d[i - 1]) || (sw2d_lt0(fW) && dc)) fW = 0;
+            if ((sw2d_gt0(fE) && dc) || (sw2d_lt0(fE) && d[i + 1])) fE = 0;
             const double ho = p.h[cur][i];
             double raw, rt;
             hn = continuity(p, i, f, ho, fS - fN, fE - fW, s.dt2, s.rr2, s.ev2, s.ql2, &raw, &rt);
             p.h[nxt][i] = hn;
             if (f & SW2D_F_ACTIVE) {
-                if (raw < 0) atomicAdd(&p.clk->led[LED_CLAMP], -raw * p.area); /* max(h, 0) gain */
+                if (sw2d_lt0(raw)) atomicAdd(&p.clk->led[LED_CLAMP], -raw * p.area); /* max(h, 0) gain */
                 if (p.ledger_cells) {
                     vr = rt;
-                    ve = (ho > p.ev_wl_min) ? s.ev2 : 0.0;
+                    ve = sw2d_gt(ho, p.ev_wl_min) ? s.ev2 : 0.0;
                 }
                 if (r == p.R - 1) vq = fS;
-                wet = hn >= p.th;
             }
         }
     }
@@ -560,7 +586,6 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_depth(StepParams p, int
         pe = block_sum(ve, smd);
     }
     if (p.outflow_south && (blockIdx.y + 1) * SW2D_BY >= p.R) pq = block_sum(vq, smd);
-    (void)wet;
     const int tid = tid_linear();
     const int b = blockIdx.y * gridDim.x + blockIdx.x;
     if (tid == 0) {
@@ -664,29 +689,27 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, i
     const double th = p.th;
     if (c < p.C) {
         double F = p.qx[nxt][i];
-        if (clip) {
-            const double F0 = F;
-            if ((F0 > 0 && d[i - P]) || (F0 < 0 && d[i])) F = 0;
-            if (F != F0) p.qx[nxt][i] = F;
+        if (clip && ((sw2d_gt0(F) && d[i - P]) || (sw2d_lt0(F) && d[i]))) {
+            F = 0;
+            p.qx[nxt][i] = F;
         }
         double hm;
         if (r == 0) hm = h[i];
         else if (r == p.R) hm = h[i - P];
-        else hm = 0.50 * (h[i] + h[i - P]);
-        p.uu1[i] = (hm >= th) ? (F == 0 ? F : F / hm) : 0.00; /* 0/hm is 0 of F's sign */
+        else hm = sw2d_half(h[i] + h[i - P]);
+        p.uu1[i] = sw2d_ge_pos(hm, th) ? (sw2d_is0(F) ? F : F / hm) : 0.00; /* 0/hm is 0 of F's sign */
     }
     if (r < p.R) {
         double F = p.qy[nxt][i];
-        if (clip) {
-            const double F0 = F;
-            if ((F0 > 0 && d[i - 1]) || (F0 < 0 && d[i])) F = 0;
-            if (F != F0) p.qy[nxt][i] = F;
+        if (clip && ((sw2d_gt0(F) && d[i - 1]) || (sw2d_lt0(F) && d[i]))) {
+            F = 0;
+            p.qy[nxt][i] = F;
         }
         double hn;
         if (c == 0) hn = h[i];
         else if (c == p.C) hn = h[i - 1];
-        else hn = 0.50 * (h[i] + h[i - 1]);
-        p.vv1[i] = (hn >= th) ? (F == 0 ? F : F / hn) : 0.0;
+        else hn = sw2d_half(h[i] + h[i - 1]);
+        p.vv1[i] = sw2d_ge_pos(hn, th) ? (sw2d_is0(F) ? F : F / hn) : 0.0;
     }
 }
 

