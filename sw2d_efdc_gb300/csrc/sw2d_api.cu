@@ -66,6 +66,8 @@ struct sw2d_handle {
     uint8_t* drys = nullptr;
     uint8_t* mcls = nullptr;
     double* mtab = nullptr;
+    double* gnn = nullptr; /* friction coefficient per class pair */
+    int ncls = 0;
     float* rainw = nullptr;
     int* src_idx = nullptr;
     double* rain = nullptr;
@@ -145,6 +147,16 @@ struct sw2d_handle {
         p.z = z;
         p.mcls = mcls;
         p.mtab = mtab;
+        p.gnn = gnn;
+        p.ncls = ncls;
+        p.gnn_uni = cfg.g * cfg.manning * cfg.manning; /* the reference's gg*rn*rn (SW2D-EFDC.cu:193) */
+        auto pow2_exp = [](double d) {
+            int k;
+            const double m = std::frexp(d, &k); /* d = m 2^k, m in [0.5, 1) */
+            return (m == 0.5 && k >= 1 && k <= 31) ? k - 1 : -1;
+        };
+        p.kdx = pow2_exp(cfg.dx);
+        p.kdy = pow2_exp(cfg.dy);
         p.rainw = rainw;
         p.src_idx = src_idx;
         p.rain = rain;
@@ -597,6 +609,7 @@ int sw2d_destroy(sw2d_handle* h) {
     dfree(h->drys);
     dfree(h->mcls);
     dfree(h->mtab);
+    dfree(h->gnn);
     dfree(h->rainw);
     dfree(h->src_idx);
     dfree(h->rain);
@@ -696,6 +709,8 @@ int sw2d_set_manning_classes(sw2d_handle* h, const uint8_t* cls, const double* t
     if (!cls) {
         dfree(h->mcls);
         dfree(h->mtab);
+        dfree(h->gnn);
+        h->ncls = 0;
         h->graph_dirty = true;
         return SW2D_OK;
     }
@@ -706,6 +721,22 @@ int sw2d_set_manning_classes(sw2d_handle* h, const uint8_t* cls, const double* t
     dfree(h->mtab);
     if ((rc = dalloc(&h->mtab, 256))) return rc;
     CK(cudaMemcpy(h->mtab, table, sizeof(double) * ntable, cudaMemcpyHostToDevice));
+    /* the friction coefficient (g n_f) n_f of every class pair, n_f the mean
+     * of the two cells' n, with the reference's operations in its order
+     * (SW2D-EFDC.cu:193, :310); up to 32 classes, else per face */
+    dfree(h->gnn);
+    h->ncls = 0;
+    if (ntable <= 32) {
+        std::vector<double> g2((size_t)ntable * ntable);
+        for (int a = 0; a < ntable; a++)
+            for (int b = 0; b < ntable; b++) {
+                const double nf = 0.50 * (table[a] + table[b]);
+                g2[(size_t)a * ntable + b] = h->cfg.g * nf * nf;
+            }
+        if ((rc = dalloc(&h->gnn, g2.size()))) return rc;
+        CK(cudaMemcpy(h->gnn, g2.data(), sizeof(double) * g2.size(), cudaMemcpyHostToDevice));
+        h->ncls = ntable;
+    }
     if ((rc = upload_interior(h, h->mcls, cls, h->R, h->C))) return rc;
     h->graph_dirty = true;
     return SW2D_OK;

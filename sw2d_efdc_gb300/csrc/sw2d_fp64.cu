@@ -126,10 +126,28 @@ __device__ __forceinline__ double face_manning(const StepParams& p, size_t a, si
     return sw2d_half(p.mtab[p.mcls[a]] + p.mtab[p.mcls[b]]);
 }
 
-__device__ __forceinline__ double friction(const StepParams& p, double nf, double sq, double hm) {
+/* (g n_f) n_f of the face between cells b and a: the reference's gg*rn*rn
+ * (:193, :310), from the class-pair table or the uniform value when the
+ * host could evaluate it once with the same operations */
+__device__ __forceinline__ double friction_coef(const StepParams& p, size_t b, size_t a) {
+    if (!p.mcls) return p.gnn_uni;
+    if (p.gnn) return p.gnn[(int)p.mcls[b] * p.ncls + (int)p.mcls[a]];
+    const double nf = face_manning(p, b, a);
+    return p.g * nf * nf;
+}
+
+__device__ __forceinline__ double friction(const StepParams& p, double coef, double sq, double hm) {
     /* :193-198; the division by pow(hm, 1.333333) as a product with hm^-1.333333 */
     if (sw2d_le_pos(hm, p.th)) return 0.00;
-    return (p.g * nf * nf * sq) * sw2d_rpow_manning(hm);
+    return (coef * sq) * sw2d_rpow_manning(hm);
+}
+
+/* a / dx for the continuity: exact scaling when dx is a power of two (the
+ * constant-division sequence returns the same bits), else sw2d_div_const */
+__device__ __forceinline__ double div_spacing(double a, double d, double rd, int k) {
+    if (k < 0) return sw2d_div_const(a, d, rd);
+    if (sw2d_is0(a)) return 0.0;
+    return k == 0 ? a : sw2d_pow2_down(a, k, rd);
 }
 
 /* Upwind donor-cell transport across the edge between two neighbouring
@@ -199,14 +217,13 @@ __device__ __forceinline__ double face_special(const FaceK& f, double th, double
 
 /* momentum update of a face (SW2D-EFDC.cu:165-202 x, :282-319 y): along /
  * across are the face's two edge differences, already scaled. */
-__device__ __forceinline__ double face_momentum(const StepParams& p, const FaceK& f, double q0, double u0,
-                                                double vt, double along, double across, double dt2,
-                                                double dt2n, size_t ia, size_t ib) {
+__device__ __forceinline__ double face_momentum(const StepParams& p, const FaceK& f, double hm, double q0,
+                                                double u0, double vt, double along, double across,
+                                                double dt2, double dt2n, size_t ia, size_t ib) {
     const double gg = p.g;
-    const double hm = sw2d_half(f.hb + f.ha);
     const double g13 = gg * hm * dt2n * (f.hhb - f.ha - f.za);
     const double sq = sqrt(u0 * u0 + vt * vt);
-    const double ram = friction(p, face_manning(p, ib, ia), sq, hm);
+    const double ram = friction(p, friction_coef(p, ib, ia), sq, hm);
     const double a = sw2d_half(dt2 * ram);
     return ((1.00 - a) * q0 + (-along - across - g13)) / (1.00 + a);
 }
@@ -300,6 +317,9 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
             if (r < p.R) p.qy[nxt][i] = vno[i];
         } else {
             const double dt2 = s.dt2, dt2dx = s.dt2dx, dt2dy = s.dt2dy, gg = p.g;
+            /* mean depths of the two faces: the momentum update and the CFL speed */
+            const double hmX = (doX && r > 0) ? sw2d_half(h[i] + h[i - P]) : 0.0;
+            const double hmY = (doY && c > 0) ? sw2d_half(h[i] + h[i - 1]) : 0.0;
             if (doX) {
                 double F;
                 if (edgeS) { /* south edge: free overfall when open */
@@ -310,7 +330,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
                     const double u11 = dt2dx * (sea[ty + 1][tx] - sea[ty][tx]);
                     const double u12 = (c == 0) ? 0.0 : dt2dy * (seb[ty][tx + 1] - seb[ty][tx]);
                     const double vt = sw2d_quarter(vv1[i] + vv1[i + 1] + vv1[i - P] + vv1[i - P + 1]);
-                    F = face_momentum(p, fx, umo[i], uu1[i], vt, u11, u12, dt2, dt2dx, i - P, i);
+                    F = face_momentum(p, fx, hmX, umo[i], uu1[i], vt, u11, u12, dt2, dt2dx, i - P, i);
                 } else {
                     F = face_special(fx, th, gg);
                 }
@@ -322,7 +342,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
                     const double v11 = (r == 0) ? 0.0 : dt2dx * (sec[ty + 1][tx] - sec[ty][tx]);
                     const double v12 = dt2dy * (sed[ty][tx + 1] - sed[ty][tx]);
                     const double ut = sw2d_quarter(uu1[i] + uu1[i + P] + uu1[i - 1] + uu1[i + P - 1]);
-                    F = face_momentum(p, fy, vno[i], vv1[i], ut, v11, v12, dt2, dt2dy, i - 1, i);
+                    F = face_momentum(p, fy, hmY, vno[i], vv1[i], ut, v11, v12, dt2, dt2dy, i - 1, i);
                 } else {
                     F = face_special(fy, th, gg);
                 }
@@ -331,12 +351,12 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
             if (p.dt_mode == 1) {
                 const uint8_t fc = p.flags[i];
                 if (c < p.C && r > 0 && r < p.R && (fc & p.flags[i - P] & SW2D_F_ACTIVE)) {
-                    hmx = sw2d_half(h[i] + h[i - P]);
+                    hmx = hmX;
                     okx = sw2d_ge_pos(hmx, th);
                     vx = uu1[i];
                 }
                 if (r < p.R && c > 0 && c < p.C && (fc & p.flags[i - 1] & SW2D_F_ACTIVE)) {
-                    hmy = sw2d_half(h[i] + h[i - 1]);
+                    hmy = hmY;
                     oky = sw2d_ge_pos(hmy, th);
                     vy = vv1[i];
                 }
@@ -370,13 +390,18 @@ __device__ __forceinline__ double continuity(const StepParams& p, size_t i, uint
         evapo = 0.000;
     }
     const double rcell = p.rainw ? rr * (double)p.rainw[i] : rr;
-    double qli = 0.0;
+    /* (((dqx/dx + dqy/dy) - q_src) - r pct) + e; subtracting a zero source
+     * and adding a zero evaporation change no value, so they are skipped */
+    double sum = div_spacing(divx, p.dx, p.rdx, p.kdx) + div_spacing(divy, p.dy, p.rdy, p.kdy);
     if (f & SW2D_F_SOURCE) {
+        double qli = 0.0;
         for (int k = 0; k < p.nsrc; k++)
             if (p.src_idx[k] == (int)i) qli = ql[k];
+        sum = sum - qli;
     }
-    double hn = ho - dt2 * (sw2d_div_const(divx, p.dx, p.rdx) + sw2d_div_const(divy, p.dy, p.rdy) - qli -
-                            rcell * pct + evapo);
+    sum = sum - rcell * pct;
+    if (p.evap) sum = sum + evapo;
+    double hn = ho - dt2 * sum;
     *raw = hn;
     *rain_term = rcell * pct;
     hn = sw2d_max0(hn);

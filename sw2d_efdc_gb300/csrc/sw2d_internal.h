@@ -81,6 +81,10 @@ struct StepParams {
     const double* z;
     const uint8_t* mcls;   /* Manning class per cell or NULL */
     const double* mtab;    /* class table (device) */
+    const double* gnn;     /* (g n_f) n_f per (class, class) pair, ncls^2, or NULL */
+    int ncls;
+    double gnn_uni;        /* (g n) n of the uniform n */
+    int kdx, kdy;          /* dx = 2^kdx (dy = 2^kdy) when a power of two >= 1, else -1 */
     const float* rainw;    /* rain weight per cell or NULL */
     const int* src_idx;    /* padded cell index per source */
     const double* rain;    /* nrain + 2 */

@@ -123,12 +123,14 @@ SW2D_HD double sw2d_scale_down(double x, int k) {
  * exponent decrement when every lane's operand is a normal number whose
  * result stays normal, and the binary64 product otherwise (both exact); the
  * host evaluates the product. */
+#if defined(__CUDACC__)
+__device__ __forceinline__ double sw2d_pow2_down(double x, int k, double m) { /* m = 2^-k, k >= 1 */
 #if defined(__CUDA_ARCH__)
-__device__ __forceinline__ double sw2d_pow2_down(double x, int k, double m) {
     const uint64_t b = sw2d_f64_bits(x);
     const uint32_t e = (uint32_t)(b >> 52) & 0x7ffu;
     if (__all_sync(__activemask(), e > (uint32_t)k && e != 0x7ffu))
         return sw2d_f64_from_bits(b - ((uint64_t)k << 52));
+#endif
     return x * m;
 }
 __device__ __forceinline__ double sw2d_half(double x) { return sw2d_pow2_down(x, 1, 0.5); }

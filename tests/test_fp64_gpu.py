@@ -93,6 +93,19 @@ def test_cfl_outflow_fields_bitwise():
     _assert_same(_fields(m), od.fields(), keys=("h", "qx", "qy"))
 
 
+@pytest.mark.parametrize("cell", [2.0, 1.0, 4.0])
+def test_power_of_two_spacing_bitwise(cell):
+    # dq/dx by an exact scaling when dx is a power of two; classes through
+    # the class-pair friction table
+    rng = np.random.default_rng(int(cell * 10))
+    case = bumpy_case(R=44, C=38, seed=17, cellsize=cell, dt=0.01, t_end=8.0)
+    case.manning_field = rng.choice([0.02, 0.05, 0.10], size=case.dem.shape)
+    m, od, ol, n = _run_pair(case)
+    g = _fields(m)
+    _assert_same(g, od.fields())
+    assert np.abs(g["h"] - ol.fields()["h"]).max() <= DH_TOL
+
+
 def test_outlet_hydrograph_matches():
     case = bumpy_case(R=40, C=32, seed=5, dt_mode=O.DT_CFL, cfl=0.7, dt_max=2.0, outflow_south=True,
                       rain_mode=O.RAIN_STEP, rain=np.array([20.0, 20.0, 0.0]), dtrain=60.0, t_end=200.0,
