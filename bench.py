@@ -34,6 +34,12 @@ sys.path.insert(0, ROOT)
 METRIC = "Gcell-updates/s plain vs batched-FP32 on 1 GB300 at stated error; p50/p99 latency"
 UNIT = "Gcell-updates/s"
 BYTES_PER_CELL_FP64_CFG2 = 62  # h,qx,qy r+w 48 + z 8 + flag 1 + Manning class 1 + rain weight (fp32) 4
+# k64_flux per cell: reads h, z, qx, qy, uu1, vv1 (6 x 8) + flag + Manning class, writes qx, qy (2 x 8)
+BYTES_PER_CELL_K64_FLUX = 66
+# DRAM bytes per cell of one k64_flux launch, 4096 x 4096 pond-break at t = 60 s: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum = 673.2 + 248.3 MB over 16.78 M cells
+# (profiles/k64_flux_4096.md)
+TRAFFIC_PER_CELL_K64_FLUX = 54.93
 BYTES_PER_CELL_FP32_CFG3 = 37  # h,qx,qy r+w 24 + z offset 4 + info byte 1 + Kahan compensation r+w 8
 
 
@@ -424,7 +430,8 @@ def run_ours(args):
 
     kernels = None
     if not args.no_kernel_split:
-        # per-kernel shares (event-timed launches outside the timed region)
+        # per-kernel launch durations: CUDA events between the four kernels on
+        # their stream over the four iterations right after the timed region
         m.set_profiling(True)
         m.step(4)
         _, kms = m.timing()
@@ -452,7 +459,26 @@ def run_ours(args):
 
     value = world * cells / (ms_iter * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    achieved = BYTES_PER_CELL_FP64_CFG2 * cells / (ms_iter * 1e-3) / 1e9
+    achieved_it = BYTES_PER_CELL_FP64_CFG2 * cells / (ms_iter * 1e-3) / 1e9
+    if kernels:
+        # the dominant kernel, k64_flux, at its event-timed launch duration
+        flux_ms = kernels["k64_flux"]["ms"]
+        roof = {"bound": "hbm", "kernel": "k64_flux",
+                "achieved": round(BYTES_PER_CELL_K64_FLUX * cells / (flux_ms * 1e-3) / 1e9, 2), "peak": peak,
+                "unit": "GB/s", "bytes_per_cell_update": BYTES_PER_CELL_K64_FLUX,
+                "launch_ms": round(flux_ms, 4), "share_of_iteration": round(kernels["k64_flux"]["share"], 4),
+                "traffic": (round(TRAFFIC_PER_CELL_K64_FLUX * cells / 1e9, 4) if TRAFFIC_PER_CELL_K64_FLUX else None),
+                "traffic_unit": "GB per launch"}
+        roof["frac"] = round(roof["achieved"] / peak, 5)
+    else:
+        roof = {"bound": "hbm", "kernel": "FP64 iteration", "achieved": round(achieved_it, 2), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved_it / peak, 5), "traffic": None,
+                "bytes_per_cell_update": BYTES_PER_CELL_FP64_CFG2}
+    roof.update({"peak_source": peak_kind,
+                 "iteration": {"achieved": round(achieved_it, 2), "bytes_per_cell_update": BYTES_PER_CELL_FP64_CFG2,
+                               "frac": round(achieved_it / peak, 5)},
+                 "note": "binary64 arithmetic bounds the FP64 step on GB300 (FP64 pipe ~85% busy in k64_flux, "
+                         "ncu), not HBM; the FP32 precision form is the HBM-bound path"})
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": round(ms_iter, 4), "higher_is_better": True, "scaling": "weak",
@@ -463,11 +489,7 @@ def run_ours(args):
                    "cells": cells, "l2": "state %.2f GB > L2 (129 MB), no flush needed" % (cells * 80 / 1e9),
                    "parallelism": "replicas" if world > 1 else "1 GPU", "timed_from_t_s": round(t_spun, 3),
                    "host_wall_ms_per_step": round(wall / K * 1e3, 4)},
-        "roofline": {"bound": "hbm", "kernel": "FP64 iteration (k64_flux+k64_hstar+k64_depth+k64_facevel)",
-                     "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 5), "traffic": None,
-                     "bytes_per_cell_update": BYTES_PER_CELL_FP64_CFG2, "peak_source": peak_kind,
-                     "note": "the FP64 step is bound by GB300's FP64 pipe, not HBM"},
+        "roofline": roof,
         "kernels": kernels,
         "gpu_launches": 4 * K,
         "clocks": clocks,
