@@ -13,6 +13,9 @@ Two products, both outside the shipped library:
   and compiled behind ``ref_shim.h`` with ``ref_driver.cpp``.  This needs the
   reference checkout; where it is absent, a previously extracted
   ``ref_kernels.inc`` is reused if present.
+* ``oracle/_ref/libsw2dref_gpu.so`` -- the same extracted kernels compiled
+  by nvcc for sm_103a and driven by ``ref_gpu_driver.cu`` with the
+  reference's own launch configuration: the "reference GPU" timing line.
 
 Run as ``python oracle/build.py`` or call :func:`build_all`.
 """
@@ -31,6 +34,7 @@ REFERENCE_CU = os.path.join(REFERENCE_ROOT, "SW2D-EFDC.cu")
 
 ORACLE_LIB = os.path.join(BUILD_DIR, "libsw2d_oracle.so")
 REF_LIB = os.path.join(REF_DIR, "libsw2dref.so")
+REF_GPU_LIB = os.path.join(REF_DIR, "libsw2dref_gpu.so")
 REF_INC = os.path.join(REF_DIR, "ref_kernels.inc")
 
 # First and one-past-last lines of the extracted range, matched by prefix.
@@ -110,6 +114,25 @@ def build_reference(force: bool = False) -> str | None:
     return REF_LIB
 
 
+def build_reference_gpu(force: bool = False) -> str | None:
+    """The same extracted kernels compiled by nvcc for sm_103a behind
+    ref_gpu_driver.cu (the reference's launch configuration and host loop):
+    the "reference GPU" timing line."""
+    if not extract_reference():
+        return None
+    srcs = [os.path.join(HERE, "ref_gpu_driver.cu"), os.path.join(HERE, "ref_case.h"), REF_INC]
+    if not force and _newer(REF_GPU_LIB, srcs):
+        return REF_GPU_LIB
+    nvcc = os.environ.get("NVCC", "nvcc")
+    if not os.path.exists(nvcc) and subprocess.run(["which", nvcc], capture_output=True).returncode != 0:
+        nvcc = "/usr/local/cuda/bin/nvcc"
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+           "-shared", "-w", "-I", HERE, "-I", REF_DIR, srcs[0], "-o", REF_GPU_LIB + ".tmp"]
+    _run(cmd)
+    os.replace(REF_GPU_LIB + ".tmp", REF_GPU_LIB)
+    return REF_GPU_LIB
+
+
 def build_all(force: bool = False) -> dict:
     out = {"oracle": build_oracle(force)}
     try:
@@ -117,6 +140,11 @@ def build_all(force: bool = False) -> dict:
     except RuntimeError as e:  # the reference build is optional on machines without it
         out["reference"] = None
         out["reference_error"] = str(e)
+    try:
+        out["reference_gpu"] = build_reference_gpu(force)
+    except (RuntimeError, OSError) as e:
+        out["reference_gpu"] = None
+        out["reference_gpu_error"] = str(e)
     return out
 
 

@@ -128,6 +128,28 @@ def ref_lib():
     return _ref
 
 
+_ref_gpu = None
+
+
+def ref_gpu_lib():
+    """The reference's own kernels compiled for the GPU, or None."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        path = _build.REF_GPU_LIB
+        if not os.path.exists(path):
+            try:
+                path = _build.build_reference_gpu()
+            except (RuntimeError, OSError):
+                path = None
+        if not path or not os.path.exists(path):
+            return None
+        L = C.CDLL(path)
+        L.sw2dref_gpu_run.argtypes = [C.POINTER(RefCase), C.POINTER(RefOut)]
+        L.sw2dref_gpu_run.restype = C.c_int
+        _ref_gpu = L
+    return _ref_gpu
+
+
 @dataclass
 class Case:
     """One SW2D problem in the reference orientation (row 0 = north)."""
@@ -284,16 +306,20 @@ def couple_values(rows, cols, dx, dy, side, cell, h, uua, vva):
 
 def run_reference(case: Case, nthreads: int = 1, mask=None, lkout: int = 0,
                   efdc_basetime: float = 3600.0, max_samples: int = 0, evap_inputs=None,
-                  sources=None, warm_iters: int = 0, want_fields: bool = True):
-    """Run the reference's own kernels (CPU build) on a case in fixed-dt mode.
+                  sources=None, warm_iters: int = 0, want_fields: bool = True, gpu: bool = False):
+    """Run the reference's own kernels (CPU build, or with ``gpu`` the nvcc
+    build on the GPU with the reference's launch configuration) on a case in
+    fixed-dt mode.
 
     Returns the reference-layout fields reshaped to (rows, cols) plus the raw
-    coupling arrays when a mask is given.  ``sources``: (brx, bry, qq, dtoq,
-    xcoor_c, ycoor_c) as the reference reads them.
+    coupling arrays when a mask is given (CPU only).  ``sources``: (brx, bry,
+    qq, dtoq, xcoor_c, ycoor_c) as the reference reads them.
     """
-    L = ref_lib()
+    L = ref_gpu_lib() if gpu else ref_lib()
     if L is None:
-        raise RuntimeError("reference CPU build unavailable")
+        raise RuntimeError("reference %s build unavailable" % ("GPU" if gpu else "CPU"))
+    if gpu and mask is not None:
+        raise ValueError("the reference GPU driver takes no coupling samples")
     R, Cc = case.rows, case.cols
     N = R * Cc + Cc // 2
     rc = RefCase()
@@ -338,9 +364,9 @@ def run_reference(case: Case, nthreads: int = 1, mask=None, lkout: int = 0,
         bc = np.zeros(4 * max(wc, 1) * 3, np.int32)
         val = np.zeros(4 * max_samples * (wc + 1))
         ro.bc, ro.val = _ptr(bc, _ip), _ptr(val, _dp)
-    rcode = L.sw2dref_run(C.byref(rc), C.byref(ro))
+    rcode = (L.sw2dref_gpu_run if gpu else L.sw2dref_run)(C.byref(rc), C.byref(ro))
     if rcode != 0:
-        raise RuntimeError("sw2dref_run failed: %d" % rcode)
+        raise RuntimeError("reference run failed: %d" % rcode)
     res = {k: v[: R * Cc].reshape(R, Cc) for k, v in outs.items()}
     res["iters"] = ro.iters
     res["time"] = ro.time
