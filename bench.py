@@ -36,10 +36,10 @@ UNIT = "Gcell-updates/s"
 BYTES_PER_CELL_FP64_CFG2 = 62  # h,qx,qy r+w 48 + z 8 + flag 1 + Manning class 1 + rain weight (fp32) 4
 # k64_flux per cell: reads h, z, qx, qy, uu1, vv1 (6 x 8) + flag + Manning class, writes qx, qy (2 x 8)
 BYTES_PER_CELL_K64_FLUX = 66
-# DRAM bytes per cell of one k64_flux launch, 4096 x 4096 pond-break at t = 60 s: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum = 673.2 + 248.3 MB over 16.78 M cells
+# DRAM bytes per cell of one k64_flux launch, 4096 x 4096 pond-break at t = 600 s: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum = 821.7 + 251.0 MB over 16.78 M cells
 # (profiles/k64_flux_4096.md)
-TRAFFIC_PER_CELL_K64_FLUX = 54.93
+TRAFFIC_PER_CELL_K64_FLUX = 63.93
 BYTES_PER_CELL_FP32_CFG3 = 37  # h,qx,qy r+w 24 + z offset 4 + info byte 1 + Kahan compensation r+w 8
 
 
