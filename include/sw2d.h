@@ -36,7 +36,8 @@ enum {
     SW2D_ERR_NUMERIC = -6,   /* non-finite depth or discharge detected */
     SW2D_ERR_NODEVICE = -7,  /* no CUDA device of compute capability 10.3 */
     SW2D_ERR_TIMEOUT = -8,   /* a bounded device wait gave up */
-    SW2D_ERR_NOT_FOUND = -9  /* unknown request id */
+    SW2D_ERR_NOT_FOUND = -9, /* unknown request id */
+    SW2D_ERR_IO = -10        /* a file could not be opened or written */
 };
 
 /* Arithmetic of the state and fluxes. */
@@ -174,6 +175,15 @@ int sw2d_get_coupling_faces(sw2d_handle* h, int* side, int* efdc_i, int* efdc_j,
  * reference's first sample (SW2D-EFDC.cu:4905).  q_out: n_faces discharges
  * (m3/s, inflow to the lake only), may be NULL. */
 int sw2d_couple_sample(sw2d_handle* h, int initial, double* q_out, int capacity);
+/* Write the EFDC inflow deck QSER.INP as write_efdc_QSER does
+ * (SW2D-EFDC.cu:2499-2610, read by EFDC_src/INPUT.F:3969-4010), byte for byte:
+ * one series per coupling face, north faces first, then south, east, west.
+ * side: n_faces sides from sw2d_get_coupling_faces; times: nsamples values of
+ * the first column (the reference's mstep*dt / efdc_basetime); q: nsamples
+ * rows of n_faces discharges from sw2d_couple_sample; each of the nlayers
+ * layers receives q / nlayers; type is the deck's InType. Host only. */
+int sw2d_write_qser(const char* path, int type, int nlayers, double efdc_basetime, int n_faces, const int* side,
+                    int nsamples, const double* times, const double* q);
 
 /* Device state snapshot (h, qx, qy, clock, ledger) to a host buffer. */
 int sw2d_snapshot_size(sw2d_handle* h, size_t* bytes);

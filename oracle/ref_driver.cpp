@@ -197,4 +197,28 @@ int sw2dref_run(const sw2dref_case* c, sw2dref_out* o) {
     return 0;
 }
 
+/* The reference's own QSER.INP writer (write_efdc_QSER, SW2D-EFDC.cu:2499-2610)
+ * on the per-side arrays sw2dref_run returns: bc is 4 x water_cells x 3,
+ * val is 4 x max_samples x (water_cells + 1); nsamples = tq + 1. */
+int sw2dref_write_qser(const char* path, int type, int nlayers, const int* bc, const double* val, int water_cells,
+                       int max_samples, double efdc_basetime, int nsamples) {
+    std::vector<int> bcs[4];
+    std::vector<double> vals[4];
+    std::vector<int*> bcp[4];
+    std::vector<double*> valp[4];
+    for (int s = 0; s < 4; s++) {
+        bcs[s].assign((size_t)(water_cells + 1) * 3, 0); /* zero row ends each side's list */
+        std::memcpy(bcs[s].data(), bc + (size_t)s * water_cells * 3, sizeof(int) * (size_t)water_cells * 3);
+        vals[s].assign(val + (size_t)s * max_samples * (water_cells + 1),
+                       val + (size_t)(s + 1) * max_samples * (water_cells + 1));
+        bcp[s].resize(water_cells + 1);
+        valp[s].resize(max_samples);
+        for (int i = 0; i <= water_cells; i++) bcp[s][i] = &bcs[s][(size_t)i * 3];
+        for (int t = 0; t < max_samples; t++) valp[s][t] = &vals[s][(size_t)t * (water_cells + 1)];
+    }
+    write_efdc_QSER(path, type, nlayers, bcp[0].data(), bcp[1].data(), bcp[2].data(), bcp[3].data(),
+                    valp[0].data(), valp[1].data(), valp[2].data(), valp[3].data(), efdc_basetime, nsamples - 1);
+    return 0;
+}
+
 } /* extern "C" */

@@ -124,6 +124,7 @@ SIGNATURES = {
     "sw2d_batch_release": (C.c_int, [C.c_void_p, C.c_int64]),
     "sw2d_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
     "sw2d_batch_last_error": (C.c_char_p, []),
+    "sw2d_write_qser": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip, C.c_int, _dp, _dp]),
     "sw2d_measure_state_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                              C.c_void_p, _dp, _dp]),
@@ -443,3 +444,13 @@ def measure_state_noalloc(dem_ptr, depth_ptr, qx_ptr, qy_ptr, rows, cols, dx, dy
                                              float(dy), float(nodata), float(th), float(g), stream or None,
                                              C.byref(vol), C.byref(spd)), "sw2d_measure_state_noalloc")
     return vol.value, spd.value
+
+
+def write_qser(path, side, times, q, type=0, nlayers=1, efdc_basetime=3600.0):
+    """Write QSER.INP for the coupling faces (`side` from Model.coupling_faces)
+    from samples `q` (nsamples x n_faces) at `times` (EFDC time units)."""
+    side = np.ascontiguousarray(side, np.int32)
+    times = np.ascontiguousarray(times, np.float64)
+    q = np.ascontiguousarray(q, np.float64).reshape(len(times), len(side))
+    _check(load().sw2d_write_qser(os.fsencode(path), int(type), int(nlayers), float(efdc_basetime), len(side),
+                                  _ptr(side, _ip), len(times), _ptr(times, _dp), _ptr(q, _dp)), "sw2d_write_qser")

@@ -467,6 +467,7 @@ const char* sw2d_status_string(int s) {
     case SW2D_ERR_NODEVICE: return "no sm_103 device";
     case SW2D_ERR_TIMEOUT: return "timeout";
     case SW2D_ERR_NOT_FOUND: return "not found";
+    case SW2D_ERR_IO: return "file error";
     default: return "unknown";
     }
 }

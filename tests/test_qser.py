@@ -1,0 +1,60 @@
+"""QSER.INP from the coupling samples, against the reference's own writer
+(write_efdc_QSER, SW2D-EFDC.cu:2499-2610, from the CPU build of the
+reference): the same bytes, for several layer counts and deck types."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from sw2d_efdc_gb300 import api
+from tests.helpers import bumpy_case
+
+
+def _reference_run():
+    case = bumpy_case(R=34, C=30, seed=15, holes=False, t_end=9.0, dt=0.05)
+    mask = np.zeros(case.dem.shape, np.int32)
+    mask[10:20, 8:22] = 1
+    mask[0:2, 12:16] = 1
+    max_samples = 16
+    ref = O.run_reference(case, nthreads=2, mask=mask, lkout=20, efdc_basetime=3600.0, max_samples=max_samples)
+    return case, mask, ref, max_samples
+
+
+@pytest.mark.parametrize("nlayers,dtype", [(1, 0), (3, 0), (2, 1)])
+def test_qser_matches_the_reference_writer(tmp_path, nlayers, dtype):
+    L = O.ref_lib()
+    if L is None:
+        pytest.skip("reference CPU build unavailable")
+    case, mask, ref, max_samples = _reference_run()
+    wc, ns = ref["water_cells"], ref["nsamples"]
+    assert ns > 2
+    bc = np.ascontiguousarray(ref["bc"], np.int32)
+    val = np.ascontiguousarray(ref["val"], np.float64)
+    L.sw2dref_write_qser.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                     ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_int]
+    a = tmp_path / "ref_QSER.INP"
+    assert L.sw2dref_write_qser(os.fsencode(a), dtype, nlayers, bc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                val.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), wc, max_samples, 3600.0,
+                                ns) == 0
+    # the same samples in this library's layout: the face list in scan order
+    # with a side per face, one row of discharges per sample
+    side, fi, fj, cell = O.couple_faces(mask)
+    q = np.zeros((ns, len(side)))
+    for s in range(4):
+        ks = np.flatnonzero(side == s)
+        for b, k in enumerate(ks, start=1):
+            q[:, k] = val[s, :ns, b]
+    times = val[0, :ns, 0]
+    b_path = tmp_path / "QSER.INP"
+    api.write_qser(b_path, side, times, q, type=dtype, nlayers=nlayers, efdc_basetime=3600.0)
+    assert a.read_bytes() == b_path.read_bytes()
+
+
+def test_qser_rejects_bad_arguments(tmp_path):
+    with pytest.raises(api.Sw2dError):
+        api.write_qser(tmp_path / "x", np.array([0, 5]), np.zeros(1), np.zeros((1, 2)))
+    with pytest.raises(api.Sw2dError):
+        api.write_qser(tmp_path / "x", np.array([0]), np.zeros(1), np.zeros((1, 1)), nlayers=0)
