@@ -184,6 +184,15 @@ int sw2d_couple_sample(sw2d_handle* h, int initial, double* q_out, int capacity)
  * layers receives q / nlayers; type is the deck's InType. Host only. */
 int sw2d_write_qser(const char* path, int type, int nlayers, double efdc_basetime, int n_faces, const int* side,
                     int nsamples, const double* times, const double* q);
+/* The dye, temperature and salinity decks of the same inflows, DSER.INP,
+ * TSER.INP, SSER.INP (kind 'D', 'T', 'S'), as write_efdc_DSER / _TSER / _SSER
+ * write them (SW2D-EFDC.cu:2383-2498, :2141-2254, :2026-2140), byte for byte:
+ * every layer of sample t of every face carries value[t] (nsamples values;
+ * the reference passes one concentration for dye and salt, a series for
+ * temperature). Host only. */
+int sw2d_write_efdc_concentration(const char* path, char kind, int type, int nlayers, double efdc_basetime,
+                                  int n_faces, const int* side, int nsamples, const double* times,
+                                  const double* value);
 
 /* Device state snapshot (h, qx, qy, clock, ledger) to a host buffer. */
 int sw2d_snapshot_size(sw2d_handle* h, size_t* bytes);

@@ -221,4 +221,32 @@ int sw2dref_write_qser(const char* path, int type, int nlayers, const int* bc, c
     return 0;
 }
 
+/* The reference's dye / temperature / salinity deck writers on the same
+ * arrays: kind 'D' (write_efdc_DSER, concentration value[0]), 'T'
+ * (write_efdc_TSER, the series value), 'S' (write_efdc_SSER, value[0]). */
+int sw2dref_write_conc(const char* path, char kind, int type, int nlayers, const int* bc, const double* val,
+                       int water_cells, int max_samples, double efdc_basetime, int nsamples, double* value) {
+    std::vector<int> bcs[4];
+    std::vector<int*> bcp[4];
+    for (int s = 0; s < 4; s++) {
+        bcs[s].assign((size_t)(water_cells + 1) * 3, 0);
+        std::memcpy(bcs[s].data(), bc + (size_t)s * water_cells * 3, sizeof(int) * (size_t)water_cells * 3);
+        bcp[s].resize(water_cells + 1);
+        for (int i = 0; i <= water_cells; i++) bcp[s][i] = &bcs[s][(size_t)i * 3];
+    }
+    std::vector<double> north(val, val + (size_t)max_samples * (water_cells + 1));
+    std::vector<double*> np(max_samples);
+    for (int t = 0; t < max_samples; t++) np[t] = &north[(size_t)t * (water_cells + 1)];
+    if (kind == 'D')
+        write_efdc_DSER(path, type, nlayers, bcp[0].data(), bcp[1].data(), bcp[2].data(), bcp[3].data(), np.data(),
+                        value[0], efdc_basetime, nsamples - 1);
+    else if (kind == 'T')
+        write_efdc_TSER(path, type, nlayers, bcp[0].data(), bcp[1].data(), bcp[2].data(), bcp[3].data(), np.data(),
+                        value, efdc_basetime, nsamples - 1);
+    else
+        write_efdc_SSER(path, type, nlayers, bcp[0].data(), bcp[1].data(), bcp[2].data(), bcp[3].data(), np.data(),
+                        value[0], efdc_basetime, nsamples - 1);
+    return 0;
+}
+
 } /* extern "C" */

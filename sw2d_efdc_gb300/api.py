@@ -124,6 +124,8 @@ SIGNATURES = {
     "sw2d_batch_release": (C.c_int, [C.c_void_p, C.c_int64]),
     "sw2d_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
     "sw2d_batch_last_error": (C.c_char_p, []),
+    "sw2d_write_efdc_concentration": (C.c_int, [C.c_char_p, C.c_char, C.c_int, C.c_int, C.c_double, C.c_int, _ip,
+                                                C.c_int, _dp, _dp]),
     "sw2d_write_qser": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip, C.c_int, _dp, _dp]),
     "sw2d_measure_state_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -454,3 +456,14 @@ def write_qser(path, side, times, q, type=0, nlayers=1, efdc_basetime=3600.0):
     q = np.ascontiguousarray(q, np.float64).reshape(len(times), len(side))
     _check(load().sw2d_write_qser(os.fsencode(path), int(type), int(nlayers), float(efdc_basetime), len(side),
                                   _ptr(side, _ip), len(times), _ptr(times, _dp), _ptr(q, _dp)), "sw2d_write_qser")
+
+
+def write_efdc_concentration(path, kind, side, times, value, type=0, nlayers=1, efdc_basetime=3600.0):
+    """Write DSER/TSER/SSER.INP (kind 'D', 'T', 'S') for the coupling faces:
+    value[t] (or one number for every sample) in every layer."""
+    side = np.ascontiguousarray(side, np.int32)
+    times = np.ascontiguousarray(times, np.float64)
+    value = np.ascontiguousarray(np.broadcast_to(np.asarray(value, np.float64), times.shape))
+    _check(load().sw2d_write_efdc_concentration(os.fsencode(path), kind.encode(), int(type), int(nlayers),
+                                                float(efdc_basetime), len(side), _ptr(side, _ip), len(times),
+                                                _ptr(times, _dp), _ptr(value, _dp)), "sw2d_write_efdc_concentration")

@@ -58,3 +58,27 @@ def test_qser_rejects_bad_arguments(tmp_path):
         api.write_qser(tmp_path / "x", np.array([0, 5]), np.zeros(1), np.zeros((1, 2)))
     with pytest.raises(api.Sw2dError):
         api.write_qser(tmp_path / "x", np.array([0]), np.zeros(1), np.zeros((1, 1)), nlayers=0)
+
+
+@pytest.mark.parametrize("kind,nlayers", [("D", 1), ("T", 2), ("S", 3)])
+def test_concentration_decks_match_the_reference_writers(tmp_path, kind, nlayers):
+    L = O.ref_lib()
+    if L is None:
+        pytest.skip("reference CPU build unavailable")
+    case, mask, ref, max_samples = _reference_run()
+    wc, ns = ref["water_cells"], ref["nsamples"]
+    bc = np.ascontiguousarray(ref["bc"], np.int32)
+    val = np.ascontiguousarray(ref["val"], np.float64)
+    value = (np.linspace(12.0, 18.5, ns) if kind == "T" else np.full(ns, 35.25)).astype(np.float64)
+    L.sw2dref_write_conc.argtypes = [ctypes.c_char_p, ctypes.c_char, ctypes.c_int, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                     ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    a = tmp_path / ("ref_%sSER.INP" % kind)
+    assert L.sw2dref_write_conc(os.fsencode(a), kind.encode(), 0, nlayers,
+                                bc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                val.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), wc, max_samples, 3600.0, ns,
+                                value.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 0
+    side, fi, fj, cell = O.couple_faces(mask)
+    b_path = tmp_path / ("%sSER.INP" % kind)
+    api.write_efdc_concentration(b_path, kind, side, val[0, :ns, 0], value, type=0, nlayers=nlayers)
+    assert a.read_bytes() == b_path.read_bytes()
