@@ -50,15 +50,17 @@ struct alignas(128) RwStage {
     float v[M_RWR][BW]; /* rows L-3 .. L+RB-2 */
 };
 
+/* the class and rain-weight rings come last, so that the variants without
+ * them launch with less shared memory (fp32_smem_bytes_variant) */
 struct SmemM {
     alignas(128) float stage[NS][NF][RB][BW];
-    ClsStage cls[NS];
-    RwStage rw[NS];
     unsigned long long bar[NS];
     float ntab[T32_MAXCLASS];
     float dd[9];
     double red[NW][4];
     float redf[NW][2];
+    ClsStage cls[NS];
+    RwStage rw[NS];
 };
 static_assert(offsetof(SmemM, stage) % 128 == 0, "TMA alignment");
 static_assert(offsetof(SmemM, cls) % 128 == 0 && sizeof(ClsStage) % 128 == 0, "TMA alignment");
@@ -67,6 +69,13 @@ static_assert((RB * BW * 4) % 128 == 0, "each staged array is whole 128-byte lin
 static_assert((BW * 4) % 16 == 0, "TMA inner extent must be a multiple of 16 bytes");
 
 size_t fp32_smem_bytes() { return sizeof(SmemM) + 128; }
+
+/* dynamic shared memory of variant k (bit 0 class raster, bit 1 rain weight):
+ * the struct up to the last ring the variant uses, plus the alignment slack */
+size_t fp32_smem_bytes_variant(int k) {
+    const size_t used = (k & 2) ? sizeof(SmemM) : (k & 1) ? offsetof(SmemM, rw) : offsetof(SmemM, cls);
+    return used + 128;
+}
 
 /* ---------------- TMA and mbarrier (inline PTX) -------------------------- */
 
@@ -820,7 +829,7 @@ int fp32_feature_class(const Scn32& d) {
 int fp32_configure_kernels() {
     for (int k = 0; k < T32_NCLASS; k++) {
         cudaError_t e = cudaFuncSetAttribute(kMarch[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)fp32_smem_bytes());
+                                             (int)fp32_smem_bytes_variant(k));
         if (e != cudaSuccess) return -1;
     }
     return 0;
@@ -830,7 +839,7 @@ void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, con
                            const int* class_n, Part32* d_part, cudaStream_t s) {
     for (int k = 0; k < T32_NCLASS; k++)
         if (class_n[k] > 0)
-            kMarch[k]<<<class_n[k], NT, fp32_smem_bytes(), s>>>(d_scn, d_work + class_first[k],
+            kMarch[k]<<<class_n[k], NT, fp32_smem_bytes_variant(k), s>>>(d_scn, d_work + class_first[k],
                                                                 d_part + class_first[k]);
     k32_finalize<<<(nscn + 3) / 4, 128, 0, s>>>(d_scn, nscn, d_part);
 }
