@@ -193,6 +193,31 @@ int sw2d_write_qser(const char* path, int type, int nlayers, double efdc_basetim
 int sw2d_write_efdc_concentration(const char* path, char kind, int type, int nlayers, double efdc_basetime,
                                   int n_faces, const int* side, int nsamples, const double* times,
                                   const double* value);
+/* Rewrite, in place in an existing EFDC.INP, the cards that depend on the
+ * boundary-face list, as write_efdc_CONFIG does (SW2D-EFDC.cu:1476-1766):
+ * C22 (number of salinity / temperature / dye series), C23 (NQSIJ, NQSER),
+ * C24 (one source row per face: north faces first, then south, east, west),
+ * C25 and C26 (one row of zeros per face).  Each card is replaced with the
+ * reference's own file surgery (find the card's first token and the next
+ * card's, write the new card, move the rest of the file behind it, blank
+ * the shortfall), so the file is byte for byte the one the reference
+ * leaves.  Faces as sw2d_get_coupling_faces returns them; salt_on, temp_on,
+ * dye_on are the setup.dat switches.  Host only. */
+int sw2d_write_efdc_cards(const char* path, int n_faces, const int* side, const int* efdc_i, const int* efdc_j,
+                          int salt_on, int temp_on, int dye_on);
+/* The DEM pre-pass of a coupled run (lake_catchment_smooth,
+ * SW2D-EFDC.cu:2766-2827), in place on rows*cols elevations in the
+ * reference orientation: catchment cells next to the lake mask (1 = lake)
+ * take the mean of their two neighbours across the mask edge, in the
+ * reference's sweep order (last raster row first, each row west to east,
+ * updated values feeding later cells).  Host only. */
+int sw2d_lake_catchment_smooth(int rows, int cols, const int* mask, double* dem);
+/* Evaporation series for sw2d_set_evaporation_series: n values in mm per
+ * dtrain from air temperature (deg C) and global radiation (W/m2), by the
+ * energy-balance method of gpu_evaporation_calc (SW2D-EFDC.cu:556-586),
+ * negative values clipped to zero.  Host only. */
+int sw2d_evaporation_series(int n, const double* temp, const double* rad, double albedo, double dtrain,
+                            double* mm_out);
 
 /* Device state snapshot (h, qx, qy, clock, ledger) to a host buffer. */
 int sw2d_snapshot_size(sw2d_handle* h, size_t* bytes);

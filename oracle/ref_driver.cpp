@@ -249,4 +249,50 @@ int sw2dref_write_conc(const char* path, char kind, int type, int nlayers, const
     return 0;
 }
 
+/* The reference's evaporation series (gpu_evaporation_calc,
+ * SW2D-EFDC.cu:556-586) over n entries, on one host thread. */
+int sw2dref_evaporation(int n, const double* temp, const double* rad, double albedo, double dtrain, double* out) {
+    gridDim.x = 1;
+    blockDim.x = 1;
+    std::vector<double> T(temp, temp + n), Rg(rad, rad + n), Rs(n), pw(n), lv(n);
+    REF_LAUNCH(gpu_evaporation_calc, albedo, T.data(), Rg.data(), Rs.data(), pw.data(), lv.data(), out, dtrain, n);
+    return 0;
+}
+
+/* The reference's DEM pre-pass of a coupled run (lake_catchment_smooth,
+ * SW2D-EFDC.cu:2766-2827), in place. */
+int sw2dref_lake_smooth(int rows, int cols, int* mask, double* baseo) {
+    lake_catchment_smooth(cols, rows, mask, baseo);
+    return 0;
+}
+
+/* The reference's EFDC.INP configuration writer (write_efdc_CONFIG,
+ * SW2D-EFDC.cu:1069-2025) on an existing EFDC.INP, with the face arrays of a
+ * coupling run (4 sides x water_cells x 3, as sw2dref_run returns them) and
+ * fixed values for the cards that do not depend on the faces. */
+int sw2dref_write_config(const char* path, const int* bc, int water_cells, int nqs, int nlayers, int salt_on,
+                         int temp_on, int dye_on) {
+    std::vector<int> bcs[4];
+    std::vector<int*> bcp[4];
+    for (int s = 0; s < 4; s++) {
+        bcs[s].assign((size_t)(water_cells + 1) * 3, 0);
+        std::memcpy(bcs[s].data(), bc + (size_t)s * water_cells * 3, sizeof(int) * (size_t)water_cells * 3);
+        bcp[s].resize(water_cells + 1);
+        for (int i = 0; i <= water_cells; i++) bcp[s][i] = &bcs[s][(size_t)i * 3];
+    }
+    int nqsij = nqs;
+    int lts_row[2] = {1, 1};
+    int* lts[1] = {lts_row};
+    write_efdc_CONFIG(path, &nqsij, nqs, bcp[0].data(), bcp[1].data(), bcp[2].data(), bcp[3].data(), nlayers,
+                      /*ncols*/ 10, /*nrows*/ 10, water_cells, /*TCON*/ 3600.0, /*TBEGIN*/ 0.0, /*TREF*/ 3600.0,
+                      /*NTC*/ 2, /*NTSPTC*/ 360, /*NTCPP*/ 2, /*NTCVB*/ 2, /*ISPPH*/ 1, /*NPPPH*/ 4, /*ISRPPH*/ 0,
+                      /*IPPHXY*/ 0, /*ISVPH*/ 1, /*NPVPH*/ 4, /*ISRVPH*/ 0, /*IVPHXY*/ 0, /*ISTMSR*/ 1, /*MLTMSR*/ 1,
+                      /*NBTMSR*/ 1, /*NSTMSR*/ 720, /*NWTMSR*/ 360, /*NTSSTSP*/ 1, /*TCTMSR*/ 1.0, /*nts_out*/ 1, lts,
+                      /*NTSSSS*/ 1, /*MTSP*/ 1, /*MTSC*/ 1, /*MTSA*/ 0, /*MTSUE*/ 1, /*MTSUT*/ 1, /*MTSU*/ 0,
+                      /*ZBRADJ*/ 0.0, /*ZBRCVRT*/ 1.0, /*HMIN*/ 0.1, /*HADJ*/ 0.0, /*HCVRT*/ 1.0, /*HDRY*/ 0.05,
+                      /*HWET*/ 0.1, /*BELADJ*/ 0.0, /*BELCVRT*/ 1.0, /*NWSER*/ 0, /*NASER*/ 1, /*DX*/ 10.0,
+                      /*DY*/ 10.0, dye_on, salt_on, temp_on, /*temp_opt*/ 1);
+    return 0;
+}
+
 } /* extern "C" */

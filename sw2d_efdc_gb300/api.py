@@ -127,6 +127,9 @@ SIGNATURES = {
     "sw2d_write_efdc_concentration": (C.c_int, [C.c_char_p, C.c_char, C.c_int, C.c_int, C.c_double, C.c_int, _ip,
                                                 C.c_int, _dp, _dp]),
     "sw2d_write_qser": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip, C.c_int, _dp, _dp]),
+    "sw2d_write_efdc_cards": (C.c_int, [C.c_char_p, C.c_int, _ip, _ip, _ip, C.c_int, C.c_int, C.c_int]),
+    "sw2d_lake_catchment_smooth": (C.c_int, [C.c_int, C.c_int, _ip, _dp]),
+    "sw2d_evaporation_series": (C.c_int, [C.c_int, _dp, _dp, C.c_double, C.c_double, _dp]),
     "sw2d_measure_state_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                              C.c_void_p, _dp, _dp]),
@@ -467,3 +470,39 @@ def write_efdc_concentration(path, kind, side, times, value, type=0, nlayers=1, 
     _check(load().sw2d_write_efdc_concentration(os.fsencode(path), kind.encode(), int(type), int(nlayers),
                                                 float(efdc_basetime), len(side), _ptr(side, _ip), len(times),
                                                 _ptr(times, _dp), _ptr(value, _dp)), "sw2d_write_efdc_concentration")
+
+
+def write_efdc_cards(path, side, efdc_i, efdc_j, salt_on=0, temp_on=0, dye_on=0):
+    """Rewrite cards C22-C26 of the EFDC.INP at `path` in place for the
+    coupling faces (`side`, `efdc_i`, `efdc_j` from Model.coupling_faces)."""
+    side = np.ascontiguousarray(side, np.int32)
+    fi = np.ascontiguousarray(efdc_i, np.int32)
+    fj = np.ascontiguousarray(efdc_j, np.int32)
+    if not (len(side) == len(fi) == len(fj)):
+        raise ValueError("side, efdc_i and efdc_j must have one entry per face")
+    _check(load().sw2d_write_efdc_cards(os.fsencode(path), len(side), _ptr(side, _ip), _ptr(fi, _ip),
+                                        _ptr(fj, _ip), int(salt_on), int(temp_on), int(dye_on)),
+           "sw2d_write_efdc_cards")
+
+
+def lake_catchment_smooth(mask, dem):
+    """The coupled run's DEM pre-pass on a (rows, cols) DEM; returns a new array."""
+    m = np.ascontiguousarray(mask, np.int32)
+    z = np.array(dem, np.float64, order="C", copy=True)
+    if m.shape != z.shape or z.ndim != 2:
+        raise ValueError("mask and dem must be the same (rows, cols) shape")
+    _check(load().sw2d_lake_catchment_smooth(z.shape[0], z.shape[1], _ptr(m, _ip), _ptr(z, _dp)),
+           "sw2d_lake_catchment_smooth")
+    return z
+
+
+def evaporation_series(temp, rad, albedo, dtrain):
+    """Evaporation in mm per dtrain from temperature (deg C) and radiation (W/m2)."""
+    T = np.ascontiguousarray(temp, np.float64)
+    Rg = np.ascontiguousarray(rad, np.float64)
+    if T.shape != Rg.shape or T.ndim != 1:
+        raise ValueError("temp and rad must be 1-D of one length")
+    out = np.zeros_like(T)
+    _check(load().sw2d_evaporation_series(len(T), _ptr(T, _dp), _ptr(Rg, _dp), float(albedo), float(dtrain),
+                                          _ptr(out, _dp)), "sw2d_evaporation_series")
+    return out

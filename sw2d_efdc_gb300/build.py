@@ -33,6 +33,7 @@ UNITS = {
     "sw2d_api.cu": [],
     "sw2d_noalloc.cu": ["--fmad=false", "-Xptxas", "-v"],
     "sw2d_efdc_io.cu": [],
+    "sw2d_case_prep.cu": ["-Xcompiler", "-ffp-contract=off"],
 }
 HEADERS = ["sw2d_internal.h", "sw2d_math.h", "sw2d_fp32.h", "sw2d_engine.h"]
 
