@@ -19,6 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libsw2d.so")
+CLI = os.path.join(OUT_DIR, "sw2d_cli")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
@@ -81,7 +82,24 @@ def build(verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
         os.replace(LIB + ".tmp", LIB)
+    build_cli()
     return LIB
+
+
+def build_cli() -> str:
+    """The case driver (csrc/sw2d_cli.cpp): host C++ linked against
+    libsw2d.so beside it (rpath $ORIGIN)."""
+    src = os.path.join(CSRC, "sw2d_cli.cpp")
+    deps = [src, LIB, os.path.join(ROOT, "include", "sw2d.h"), __file__]
+    if _stale(CLI, deps):
+        cxx = shutil.which("g++") or "g++"
+        cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include"), src,
+               "-o", CLI + ".tmp", "-L", OUT_DIR, "-lsw2d", "-Wl,-rpath,$ORIGIN", "-pthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("sw2d_cli build failed:\n%s\n%s" % (r.stdout, r.stderr))
+        os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 if __name__ == "__main__":
