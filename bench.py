@@ -323,7 +323,7 @@ def make_batch_specs(n, lo, hi, seed, t_scale=1.0):
 
 
 def run_batched_leg(args, peak, fp64_value):
-    """configs[3]: 256 scenarios of uneven size advanced together, one fused
+    """The batched form: 256 scenarios of uneven size advanced together, one fused
     launch per iteration (graph-captured chunks), each with its own CFL length."""
     from sw2d_efdc_gb300 import api
     t0 = time.time()
@@ -356,7 +356,7 @@ def run_batched_leg(args, peak, fp64_value):
 
 
 def run_served_leg(args, fp64_value):
-    """configs[4]: a finite Poisson trace of requests (lambda 20/s, side
+    """The served form: a finite Poisson trace of requests (lambda 20/s, side
     log-uniform 256-4096) admitted against an HBM budget as they arrive and
     advanced step by step together; completion latency = finish - arrival."""
     from sw2d_efdc_gb300 import api, synth
