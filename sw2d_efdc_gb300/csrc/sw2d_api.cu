@@ -104,9 +104,12 @@ struct sw2d_handle {
     /* FP32 precision form: a one-scenario engine built from host copies of the inputs */
     std::unique_ptr<sw2d::Engine32> eng;
     int eng_idx = -1;
-    std::vector<double> in_dem, in_depth, in_mtab, in_rain;
+    std::vector<double> in_dem, in_depth, in_mtab, in_rain, in_evap, in_srcq;
     std::vector<uint8_t> in_mcls;
     std::vector<float> in_rainw;
+    std::vector<int> in_srcc;
+    int in_nq = 0;
+    double in_dtoq = 3600.0;
     bool fp32() const { return cfg.precision == SW2D_FP32; }
 
     StepParams params() const {
@@ -348,6 +351,17 @@ int fp32_rebuild(sw2d_handle* h) {
     in.nrain = (int)h->in_rain.size();
     in.dtrain = h->dtrain;
     if (!h->in_rainw.empty()) in.rain_weight = h->in_rainw.data();
+    if (!h->in_evap.empty()) {
+        in.evap = h->in_evap.data();
+        in.nevap = (int)h->in_evap.size();
+    }
+    if (!h->in_srcc.empty()) {
+        in.nsrc = (int)h->in_srcc.size();
+        in.src_cells = h->in_srcc.data();
+        in.src_q = h->in_srcq.data();
+        in.nq = h->in_nq;
+        in.dtoq = h->in_dtoq;
+    }
     in.outlet_cap = h->outlet_cap;
     std::string err;
     int rc = h->eng->add(in, 0, &err, &h->eng_idx);
@@ -788,7 +802,10 @@ int sw2d_set_rain_field(sw2d_handle* h, const float* w) {
 
 int sw2d_set_evaporation_series(sw2d_handle* h, const double* mm, int n) {
     if (!h || n < 0 || (n > 0 && !mm)) return fail(SW2D_ERR_INVALID, "evaporation series");
-    if (h->fp32()) return fail(SW2D_ERR_STATE, "evaporation series: FP64 precision only");
+    if (h->fp32()) {
+        h->in_evap.assign(mm, mm + n);
+        return h->have_depth ? fp32_rebuild(h) : SW2D_OK;
+    }
     int rc = set_device(h);
     if (rc) return rc;
     dfree(h->evap);
@@ -805,10 +822,18 @@ int sw2d_set_evaporation_series(sw2d_handle* h, const double* mm, int n) {
 }
 
 int sw2d_set_point_sources(sw2d_handle* h, int nsrc, const int* cells, const double* q, int nq, double dtoq) {
-    if (h && h->fp32()) return fail(SW2D_ERR_STATE, "point sources: FP64 precision only");
     if (!h || nsrc < 0 || nsrc > SW2D_MAX_SRC || (nsrc > 0 && (!cells || !q || nq <= 0 || !(dtoq > 0))))
         return fail(SW2D_ERR_INVALID, "point sources");
     if (!h->have_dem) return fail(SW2D_ERR_STATE, "set_dem first");
+    if (h->fp32()) {
+        for (int k = 0; k < nsrc; k++)
+            if (cells[k] < 0 || cells[k] >= h->R * h->C) return fail(SW2D_ERR_INVALID, "source cell out of range");
+        h->in_srcc.assign(cells, cells + nsrc);
+        h->in_srcq.assign(q, q + (size_t)nq * nsrc);
+        h->in_nq = nsrc > 0 ? nq : 0;
+        h->in_dtoq = nsrc > 0 ? dtoq : 3600.0;
+        return h->have_depth ? fp32_rebuild(h) : SW2D_OK;
+    }
     int rc = set_device(h);
     if (rc) return rc;
     for (size_t i = 0; i < h->ncell; i++) h->host_flags[i] &= (uint8_t)~SW2D_F_SOURCE;

@@ -238,7 +238,41 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     if ((rc = alloc((size_t)(nrain + 2) * 8, &p))) return fail_free(rc);
     drain = (double*)p;
     d.rain = drain;
-    d.evap = nullptr;
+    /* evaporation series and point sources (a later source on a cell
+     * replaces an earlier one, as the reference's stream_flow writes them) */
+    double* devap = nullptr;
+    if (in.evap && in.nevap > 0) {
+        if ((rc = alloc((size_t)(in.nevap + 2) * 8, &p))) return fail_free(rc);
+        devap = (double*)p;
+    }
+    std::vector<int> src_keep;
+    if (in.nsrc > 0) {
+        if (in.nsrc > T32_MAXSRC || !in.src_cells || !in.src_q || in.nq <= 0 || !(in.dtoq > 0)) {
+            if (err) *err = "point sources";
+            return fail_free(SW2D_ERR_INVALID);
+        }
+        for (int k = 0; k < in.nsrc; k++) {
+            if (in.src_cells[k] < 0 || in.src_cells[k] >= R * C) {
+                if (err) *err = "source cell out of range";
+                return fail_free(SW2D_ERR_INVALID);
+            }
+            bool later = false;
+            for (int j = k + 1; j < in.nsrc; j++) later |= in.src_cells[j] == in.src_cells[k];
+            if (!later) src_keep.push_back(k);
+        }
+    }
+    const int nu = (int)src_keep.size();
+    int* dsrc_cell = nullptr;
+    double* dsrcq = nullptr;
+    if (nu > 0) {
+        if ((rc = alloc((size_t)nu * 4, &p))) return fail_free(rc);
+        dsrc_cell = (int*)p;
+        if ((rc = alloc((size_t)(in.nq + 2) * nu * 8, &p))) return fail_free(rc);
+        dsrcq = (double*)p;
+    }
+    d.evap = devap;
+    d.srcq = dsrcq;
+    d.src_cell = dsrc_cell;
     d.outlet = nullptr;
     if (in.outlet_cap > 0) {
         if ((rc = alloc((size_t)in.outlet_cap * 16, &p))) return fail_free(rc);
@@ -299,6 +333,22 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     std::vector<double> rain(nrain + 2, 0.0);
     for (int k = 0; k < in.nrain; k++) rain[k] = in.rain[k];
     ECK(cudaMemcpyAsync(drain, rain.data(), rain.size() * 8, cudaMemcpyHostToDevice, stream_));
+    std::vector<double> evap, srcq;
+    std::vector<int> srcc;
+    if (devap) {
+        evap.assign((size_t)in.nevap + 2, 0.0);
+        for (int k = 0; k < in.nevap; k++) evap[k] = in.evap[k];
+        ECK(cudaMemcpyAsync(devap, evap.data(), evap.size() * 8, cudaMemcpyHostToDevice, stream_));
+    }
+    if (nu > 0) {
+        srcq.assign((size_t)(in.nq + 2) * nu, 0.0);
+        for (int u = 0; u < nu; u++) {
+            srcc.push_back(in.src_cells[src_keep[u]]);
+            for (int t = 0; t < in.nq; t++) srcq[(size_t)t * nu + u] = in.src_q[(size_t)t * in.nsrc + src_keep[u]];
+        }
+        ECK(cudaMemcpyAsync(dsrc_cell, srcc.data(), srcc.size() * 4, cudaMemcpyHostToDevice, stream_));
+        ECK(cudaMemcpyAsync(dsrcq, srcq.data(), srcq.size() * 8, cudaMemcpyHostToDevice, stream_));
+    }
 
     /* tensor maps: rows of 232 columns, four rows per staged block; the bed
      * reads NaN (inactive) outside the array */
@@ -326,7 +376,10 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     d.series_mode = in.series_mode;
     d.dt_mode = in.dt_mode;
     d.nrain = nrain;
-    d.nevap = 0;
+    d.nevap = devap ? in.nevap : 0;
+    d.nsrc = nu;
+    d.nq = nu > 0 ? in.nq : 0;
+    d.dtoq = nu > 0 ? in.dtoq : 3600.0;
     d.outlet_cap = in.outlet_cap;
     d.dx = (float)in.dx;
     d.dy = (float)in.dy;
@@ -338,7 +391,7 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     d.pct_lake = (float)pct_lake;
     d.pct_land = (float)pct_land;
     d.ev_wl_min = (float)in.ev_wl_min;
-    d.ledger_cells = pct_lake != pct_land;
+    d.ledger_cells = pct_lake != pct_land || devap != nullptr; /* evaporation acts on lake cells only */
     d.rain_static = active_weight * pct_land;
     d.dxd = in.dx;
     d.dyd = in.dy;

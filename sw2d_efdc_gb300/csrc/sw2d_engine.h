@@ -29,6 +29,13 @@ struct ScenarioInput {
     int nrain = 0;
     double dtrain = 3600.0;
     const float* rain_weight = nullptr; /* rows*cols or NULL */
+    const double* evap = nullptr;       /* evaporation, mm per dtrain, or NULL */
+    int nevap = 0;
+    int nsrc = 0;                       /* point sources (at most T32_MAXSRC) */
+    const int* src_cells = nullptr;     /* nsrc raster ids (row*cols + col) */
+    const double* src_q = nullptr;      /* nq rows of nsrc discharges, m3/s */
+    int nq = 0;
+    double dtoq = 3600.0;
     int outlet_cap = 0;
 };
 

@@ -59,6 +59,9 @@ struct SmemM {
     float dd[9];
     double red[NW][4];
     float redf[NW][2];
+    int nls;                    /* point sources inside the work item's staged window */
+    int srow[T32_MAXSRC], scol[T32_MAXSRC];
+    float sq1[T32_MAXSRC], sq2[T32_MAXSRC];
     ClsStage cls[NS];
     RwStage rw[NS];
 };
@@ -253,8 +256,9 @@ __device__ __forceinline__ float2 face_flux2(const Face2& f, float th, float g, 
 
 /* CLS: the scenario has a Manning-class raster; RW: a rain-weight field;
  * LAKE: lake cells (depth > ev_wl_min) lose a different fraction of the rain
- * than land cells (the per-cell ledger is then kept too). */
-template <bool CLS, bool RW, bool LAKE>
+ * than land cells, or evaporate (the per-cell ledger is then kept too);
+ * SRC: point sources. */
+template <bool CLS, bool RW, bool LAKE, bool SRC>
 __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scns, const int4* __restrict__ work,
                                                    Part32* __restrict__ part) {
     extern __shared__ unsigned char smem_raw[];
@@ -288,6 +292,32 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (tid < T32_MAXCLASS) S.ntab[tid] = P.ntab[tid];
+    if (SRC && warp == 0) {
+        /* the point sources inside the staged window (rows rs-3 .. re+2,
+         * the strip's staged columns), in source order */
+        int n = 0;
+        for (int k0 = 0; k0 < P.nsrc; k0 += 32) {
+            const int k = k0 + lane;
+            int r = 0, c = 0;
+            bool in = false;
+            if (k < P.nsrc) {
+                const int cell = P.src_cell[k];
+                r = cell / C;
+                c = cell - r * C;
+                in = r >= rs - 3 && r < re + 3 && c >= c0 - M_H && c < c0 - M_H + BW;
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, in);
+            if (in) {
+                const int at = n + __popc(b & ((1u << lane) - 1u));
+                S.srow[at] = r;
+                S.scol[at] = c;
+                S.sq1[at] = clk->ql1[k];
+                S.sq2[at] = clk->ql2[k];
+            }
+            n += __popc(b);
+        }
+        if (lane == 0) S.nls = n;
+    }
     if (tid < 9) {
         const int dy = tid / 3 - 1, dx = tid % 3 - 1;
         const int ny = seg + dy, nx = strip + dx;
@@ -354,6 +384,17 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
     }
     float clamp = 0.f, qout = 0.f, rainacc = 0.f, evc = 0.f;
     float sxm = 0.f, sym = 0.f;
+    const int nls = SRC ? S.nls : 0;
+    /* point-source rates of the lane's two cells in row `row` (distinct cells) */
+    auto point_src = [&](int row, const float* q) {
+        float2 v = f2(0.f);
+        for (int k = 0; k < nls; k++)
+            if (S.srow[k] == row) {
+                if (S.scol[k] == cg) v.x += q[k];
+                if (S.scol[k] == cg + 1) v.y += q[k];
+            }
+        return v;
+    };
 
     for (int b = 0; b < nblk; b++) {
         const int st = b % NS;
@@ -491,6 +532,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 }
                 if (has_rw) src = mul2(src, *reinterpret_cast<const float2*>(srw + (j + 1) * BW + sc));
                 if (lakefx) src = sub2(src, sel2(lake, f2(ev1), f2(0.f)));
+                if (SRC && nls) src = add2(src, point_src(L - 2, S.sq1));
                 const float2 div = fma2(sub2(FX[s1], FX[s2]), f2(rdxy.x), mul2(sub2(FYR[s2], FY[s2]), f2(rdxy.y)));
                 const float2 hs = fma2(sub2(div, src), f2(-dt2), ho);
                 DRY[s2] = ACT[s2] & mask2(lt2(hs, th));
@@ -511,6 +553,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 const float2 wgt = RW ? *reinterpret_cast<const float2*>(srw + j * BW + sc) : f2(1.f);
                 if (RW) src = mul2(src, wgt);
                 if (LAKE) src = sub2(src, sel2(lake, f2(ev2), f2(0.f)));
+                if (SRC && nls) src = add2(src, point_src(r, S.sq2));
                 const float2 div = fma2(sub2(fS, fN), f2(rdxy.x), mul2(sub2(fE, fW), f2(rdxy.y)));
                 const float2 dh = mul2(sub2(div, src), f2(-dt2));
                 /* Kahan: the increment is small against the depth */
@@ -634,14 +677,38 @@ __device__ double series_at32(const double* v, int n, double dts, double time, i
     return v[it];
 }
 
+/* point-source rate (m/s) of source i at time t: the reference's stream_flow
+ * interpolation (SW2D-EFDC.cu:531-538) in REFERENCE mode, else LINEAR / STEP */
+__device__ float source_at32(const Scn32& P, int i, double time) {
+    const double* Q = P.srcq;
+    const int ns = P.nsrc;
+    double q;
+    if (P.series_mode == 0 && time <= 1.00) {
+        q = Q[i] * time;
+    } else {
+        int it = (int)(time / P.dtoq);
+        if (it + 1 > P.nq) it = P.nq;
+        const double a = Q[(size_t)it * ns + i], b = Q[(size_t)(it + 1) * ns + i];
+        if (P.series_mode == 0)
+            q = a + (b - a) / (P.dtoq * (time - P.dtoq * (it)));
+        else if (P.series_mode == 1)
+            q = a + (b - a) * ((time - P.dtoq * (it)) / P.dtoq);
+        else
+            q = a;
+    }
+    return (float)(q / (P.dxd * P.dyd));
+}
+
 __device__ void prepare_slot32(const Scn32& P, Clock32* clk) {
     const double t = clk->t;
     double dt2, tm;
     int active;
     if (P.dt_mode == 0) {
+        /* the reference's time grid: the clock advances by dt twice, as the
+         * FP64 path's; only the state update uses dt2 rounded to binary32 */
         const double dt = P.dt_fixed;
         active = (t + dt <= clk->t_end);
-        dt2 = (double)(float)(2.0 * dt);
+        dt2 = 2.0 * dt;
         tm = t + dt;
     } else {
         active = (t < clk->t_end);
@@ -662,6 +729,10 @@ __device__ void prepare_slot32(const Scn32& P, Clock32* clk) {
         s.ev2 = (float)(series_at32(P.evap, P.nevap, P.dtrain, tm, P.series_mode) / (P.dtrain * 1000.0));
     } else {
         s.ev1 = s.ev2 = 0.f;
+    }
+    for (int k = 0; k < P.nsrc; k++) {
+        clk->ql1[k] = source_at32(P, k, t);
+        clk->ql2[k] = source_at32(P, k, tm);
     }
     clk->dt2 = dt2;
     if (!active) clk->done = 1;
@@ -702,13 +773,16 @@ __global__ void k32_finalize(const Scn32* __restrict__ scns, int nscn, const Par
     const double rain_sum = P.ledger_cells ? rain : P.rain_static;
     clk->rain_in += dt2 * (double)sl.rr2 * rain_sum * area;
     clk->evap_out += dt2 * (double)sl.ev2 * evc * area;
+    double qsrc = 0.0;
+    for (int k = 0; k < P.nsrc; k++) qsrc += (double)clk->ql2[k];
+    clk->source_in += dt2 * qsrc * area;
     clk->clamp_gain += clamp * area;
     clk->q_out = qout * P.dyd;
     clk->outflow += dt2 * clk->q_out;
     /* the CFL speed of the state this iteration started from */
     clk->s_max = (double)sx + (double)sy;
     if (!isfinite(clk->s_max) || !isfinite(qout)) clk->status |= 1;
-    clk->t = clk->t + dt2;
+    clk->t = (P.dt_mode == 0) ? (clk->t + P.dt_fixed) + P.dt_fixed : clk->t + dt2;
     clk->iters += 1;
     clk->slot.cur = sl.cur ^ 1;
     if (P.outlet) {
@@ -817,13 +891,18 @@ size_t fp32_volume_scratch_bytes() { return 32 + kVolBlocks * sizeof(VolPart); }
 
 typedef void (*MarchFn)(const Scn32*, const int4*, Part32*);
 static const MarchFn kMarch[T32_NCLASS] = {
-    k32_march<false, false, false>, k32_march<true, false, false>, k32_march<false, true, false>,
-    k32_march<true, true, false>,   k32_march<false, false, true>,  k32_march<true, false, true>,
-    k32_march<false, true, true>,   k32_march<true, true, true>,
+    k32_march<false, false, false, false>, k32_march<true, false, false, false>,
+    k32_march<false, true, false, false>,  k32_march<true, true, false, false>,
+    k32_march<false, false, true, false>,  k32_march<true, false, true, false>,
+    k32_march<false, true, true, false>,   k32_march<true, true, true, false>,
+    k32_march<false, false, false, true>,  k32_march<true, false, false, true>,
+    k32_march<false, true, false, true>,   k32_march<true, true, false, true>,
+    k32_march<false, false, true, true>,   k32_march<true, false, true, true>,
+    k32_march<false, true, true, true>,    k32_march<true, true, true, true>,
 };
 
 int fp32_feature_class(const Scn32& d) {
-    return (d.cls ? 1 : 0) | (d.rainw ? 2 : 0) | (d.ledger_cells ? 4 : 0);
+    return (d.cls ? 1 : 0) | (d.rainw ? 2 : 0) | (d.ledger_cells ? 4 : 0) | (d.nsrc > 0 ? 8 : 0);
 }
 
 int fp32_configure_kernels() {

@@ -34,6 +34,7 @@ constexpr int M_CLSW = 240;            /* staged Manning-class columns (bytes; a
 constexpr int M_CLSR = M_RB + 2;       /* class rows per block: the block's rows and the two above */
 constexpr int M_RWR = M_RB + 1;        /* rain-weight rows per block: from three rows above the block */
 constexpr int T32_MAXCLASS = 64;
+constexpr int T32_MAXSRC = 64;         /* point sources per scenario */
 
 /* Length and forcing of a scenario's next iteration, written by the
  * finalize kernel, read by every work item of the scenario. */
@@ -56,6 +57,7 @@ struct Clock32 {
     int status;               /* bit 0 non-finite, bit 1 TMA wait timeout, bit 2 misaligned staging */
     int done;                 /* set when t reached t_end */
     long long outlet_n;
+    float ql1[T32_MAXSRC], ql2[T32_MAXSRC]; /* point-source rates (m/s) at the slot's two times */
 };
 
 /* per work item reduction results */
@@ -81,12 +83,16 @@ struct Scn32 {
     const float* rainw;    /* per cell (padded) or NULL */
     const double* rain;    /* nrain + 2, mm per dtrain */
     const double* evap;    /* nevap + 2 or NULL */
+    const double* srcq;    /* point-source discharges, (nq + 2) rows of nsrc, m3/s, or NULL */
+    const int* src_cell;   /* nsrc raster ids (row * C + col), distinct */
     double* outlet;        /* outlet ring (t, Q) or NULL */
     Clock32* clk;
     int R, C, P, tiles_x, tiles_y, seg;
     int first_work, nwork;
     int outflow_south, ledger_cells, series_mode, dt_mode;
     int nrain, nevap, outlet_cap;
+    int nsrc, nq;
+    double dtoq;
     float dx, dy, rdx, rdy, th, g;
     float pct_lake, pct_land, ev_wl_min;
     double rain_static;    /* sum over active cells of weight * runoff fraction */
@@ -95,9 +101,10 @@ struct Scn32 {
 };
 
 /* Feature class of a scenario (bit 0 class raster, bit 1 rain-weight field,
- * bit 2 lake fraction): the marching kernel is specialised per class and
- * the work list holds each class's items contiguously. */
-constexpr int T32_NCLASS = 8;
+ * bit 2 lake fraction or evaporation, bit 3 point sources): the marching
+ * kernel is specialised per class and the work list holds each class's
+ * items contiguously. */
+constexpr int T32_NCLASS = 16;
 int fp32_feature_class(const Scn32& d);
 void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, const int* class_first,
                            const int* class_n, Part32* d_part, cudaStream_t s);

@@ -535,7 +535,8 @@ __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
             const double dt2 = s.dt2;
             const double smax = __longlong_as_double((long long)ux) + __longlong_as_double((long long)uy);
             double src = 0.0;
-            for (int k = 0; k < p.nsrc; k++) src += s.ql2[k];
+            for (int k = 0; k < p.nsrc; k++) /* a source overridden on its cell adds nothing */
+                if (p.src_idx[k] >= 0) src += s.ql2[k];
             const double rain = p.ledger_cells ? vr : s.rr2 * p.rain_static;
             clk->led[LED_RAIN] += dt2 * rain * p.area;
             clk->led[LED_EVAP] += dt2 * ve * p.area;

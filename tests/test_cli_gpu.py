@@ -108,3 +108,28 @@ def test_cli_coupled_case_writes_the_hand_off(tmp_path):
         assert (edir / n).read_bytes() == (want / n).read_bytes(), n
     # the DEM the run used is the smoothed one (Elevations field)
     assert not np.array_equal(extra["dem"], dem)
+
+
+def test_cli_fp32_form_stays_within_a_millimetre(tmp_path):
+    """--fp32 runs the same case in the binary32 precision form: the depths
+    in the VTK files are within 1 mm of the reference's (the oracle's)."""
+    c = small_case(name="fp32", evaporation_on=1, temp=np.array([20.0, 24.0, 18.0, 15.0]),
+                   rad=np.array([400.0, 650.0, 120.0, 0.0]), frac_int=0.1, frac_inf=0.2, frac_lwl=0.05,
+                   end=(0, 0, 0, 12), dkout=4.0)
+    D.write_db(tmp_path, [c])
+    r = subprocess.run([cli(), "--root", str(tmp_path), "--fp32", "--quiet"], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    files, _ = D.expected_outputs(c)
+    odir = tmp_path / "db" / c.name / "SW2D" / "output"
+    for n, want in files.items():
+        if not n.startswith("Results_") or n == "Results_0.vtk":
+            continue
+        got = (odir / n).read_text().splitlines()
+        exp = want.decode().splitlines()
+        assert len(got) == len(exp) and got[:10] == exp[:10]
+        k = exp.index("SCALARS depth float 1") + 2
+        n_cells = c.rows * c.cols
+        dg = np.array(got[k:k + n_cells], float)
+        de = np.array(exp[k:k + n_cells], float)
+        assert np.abs(dg - de).max() < 1e-3, n

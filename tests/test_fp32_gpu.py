@@ -104,3 +104,52 @@ def test_fp32_work_item_rows_change_results_only_by_rounding(monkeypatch):
         depths.append(m.depth())
         m.close()
     assert np.abs(depths[0] - depths[1]).max() < 1e-5
+
+
+@pytest.mark.parametrize("rows", ["64", "128"])
+def test_fp32_point_sources_and_lake_evaporation(monkeypatch, rows):
+    """Point sources (one duplicated cell: the later one applies; sinks too)
+    on both sides of a strip edge (columns 223 | 224) and of a work item's
+    row edge, evaporation on lake cells and the three loss fractions: FP32
+    tracks FP64 and both ledgers balance."""
+    monkeypatch.setenv("SW2D_SEGMENT_ROWS", rows)
+    R, C = 200, 300
+    case = bumpy_case(R=R, C=C, seed=26, t_end=60.0, dt=0.05, holes=False, frac_int=0.1, frac_inf=0.2,
+                      frac_lwl=0.05, ev_wl_min=0.02, rain=np.array([6.0, 6.0, 0.0, 0.0]), dtrain=30.0)
+    case.evap = np.array([2.0, 3.0, 1.0, 0.5])  # on the ponds deeper than ev_wl_min
+    cells = [(63, 223), (64, 224), (127, 20), (128, 21), (15, 10), (12, 7), (63, 223)]  # the sink in a pond
+    case.src_cell = np.array([r * C + c for r, c in cells], np.int32)
+    case.src_q = np.array([[0.5, 0.4, 0.3, 0.2, -0.05, 0.1, 0.8],
+                           [0.6, 0.2, 0.1, 0.3, -0.02, 0.0, 0.9],
+                           [0.0, 0.1, 0.2, 0.0, 0.00, 0.2, 0.0]])
+    case.dtoq = 30.0
+    m64, m32, n64, n32 = _pair(case)
+    assert n64 == n32
+    h64, h32 = m64.depth(), m32.depth()
+    assert np.abs(h64 - h32).max() < DEPTH_TOL
+    for r, c in cells[:4]:
+        assert h32[r, c] > 0.01  # the sources did feed their cells
+    l64, l32 = m64.ledger(), m32.ledger()
+    assert l32["source_in"] == pytest.approx(l64["source_in"], rel=1e-6)
+    assert l32["evap_out"] == pytest.approx(l64["evap_out"], rel=1e-3)
+    assert l64["evap_out"] > 0
+    assert abs(l64["balance_error"]) < 1e-6 and abs(l32["balance_error"]) < 1e-6
+
+
+def test_fp32_fixed_dt_clock_follows_the_reference_time_grid():
+    """FIXED dt: the FP32 clock advances by dt twice per iteration like the
+    FP64 path, so the series are evaluated at the same times.  The reference's
+    REFERENCE interpolation divides by the time elapsed since the last series
+    entry, which is ill-conditioned just after each entry (t = 30 s here); a
+    clock that advanced by dt2 rounded to binary32 drifted by 4.5e-7 s by
+    then and saw a different rain spike (3.4 cm apart behind a dam break
+    across a strip edge)."""
+    R, C = 200, 300
+    case = bumpy_case(R=R, C=C, seed=26, t_end=60.0, dt=0.05, holes=False, rain=np.array([6.0, 6.0, 0.0, 0.0]),
+                      dtrain=30.0)
+    case.h0[:] = 0
+    case.h0[10:50, 200:260] = 0.4
+    m64, m32, n64, n32 = _pair(case)
+    assert n64 == n32
+    assert m32.time()[0] == m64.time()[0]
+    assert np.abs(m64.depth() - m32.depth()).max() < DEPTH_TOL
