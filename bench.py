@@ -71,6 +71,24 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
 
 
+def device():
+    """The GPU of this rank: replicas run one per GPU, rank i on local GPU i."""
+    return dist_env()[1]
+
+
+def rank_max(x: float) -> float:
+    """Maximum of x over all ranks (the slowest replica sets the job's time);
+    x itself with one rank.  The ranks share no data, only this scalar, over
+    the host process group."""
+    if dist_env()[2] <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region."""
 
@@ -143,7 +161,7 @@ def workload_config2(size: int = 4096):
 
 def make_model(sc):
     from sw2d_efdc_gb300 import api
-    cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=api.FP64, dt_mode=sc.dt_mode,
+    cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=api.FP64, dt_mode=sc.dt_mode, device=device(),
                              series_mode=sc.series_mode, dx=sc.dx, dy=sc.dx, manning=sc.manning,
                              cfl=sc.cfl, dt_max=sc.dt_max, dt=sc.dt,
                              outflow=api.OUTFLOW_SOUTH if sc.outflow_south else api.OUTFLOW_NONE)
@@ -209,7 +227,7 @@ def run_fp32_leg(args, peak):
     from sw2d_efdc_gb300 import api, synth
     size = args.fp32_size
     sc = synth.config3(rows=size, cols=size)
-    cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=api.FP32, dt_mode=sc.dt_mode,
+    cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=api.FP32, dt_mode=sc.dt_mode, device=device(),
                              series_mode=sc.series_mode, dx=sc.dx, dy=sc.dx, manning=sc.manning, cfl=sc.cfl,
                              dt_max=sc.dt_max, outflow=api.OUTFLOW_SOUTH)
     m = api.Model(cfg)
@@ -257,7 +275,7 @@ def run_precision_leg(args):
     # error, against which the FP32 errors are read
     for key, prec, rscale in (("fp64", api.FP64, 1.0), ("fp64_perturbed", api.FP64, 1.0 + 1e-6),
                               ("fp32", api.FP32, 1.0)):
-        cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=prec, dt_mode=sc.dt_mode,
+        cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=prec, dt_mode=sc.dt_mode, device=device(),
                                  series_mode=sc.series_mode, dx=sc.dx, dy=sc.dx, manning=sc.manning, cfl=sc.cfl,
                                  dt_max=sc.dt_max, outflow=api.OUTFLOW_SOUTH)
         m = api.Model(cfg)
@@ -329,7 +347,7 @@ def run_batched_leg(args, peak, fp64_value):
     t0 = time.time()
     specs = make_batch_specs(args.batch_n, 128, 2048, 4)
     gen_s = time.time() - t0
-    b = api.Batch()
+    b = api.Batch(device=device())
     for sp in specs:
         b.submit(**sp)
     b.step(0)
@@ -366,7 +384,7 @@ def run_served_leg(args, fp64_value):
     t0 = time.time()
     specs = make_batch_specs(n, 256, 4096, 6, t_scale=args.serve_time_scale)
     gen_s = time.time() - t0
-    b = api.Batch(hbm_budget_bytes=150e9)
+    b = api.Batch(device=device(), hbm_budget_bytes=150e9)
     ids = {}
     done = {}
     admitted = {}
@@ -450,12 +468,7 @@ def run_ours(args):
         wall = time.perf_counter() - t0
     ms_iter, _ = m.timing()
     barrier()
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        tt = torch.tensor([ms_iter], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_iter = float(tt.item())
+    ms_iter = rank_max(ms_iter)
     clocks = cs.summary()
     led = m.ledger()
 
