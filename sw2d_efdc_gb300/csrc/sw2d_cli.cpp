@@ -516,6 +516,23 @@ struct Options {
     int device = 0;
 };
 
+std::string json_str(const std::string& v) {
+    std::string o;
+    for (unsigned char ch : v) {
+        if (ch == '"' || ch == '\\') {
+            o += '\\';
+            o += (char)ch;
+        } else if (ch < 0x20) {
+            char b[8];
+            std::snprintf(b, sizeof b, "\\u%04x", ch);
+            o += b;
+        } else {
+            o += (char)ch;
+        }
+    }
+    return o;
+}
+
 void print_check(const Case& c, const std::vector<Event>& ev, long long iters) {
     std::printf("{\"case\": \"%s\", \"rows\": %d, \"cols\": %d, \"cellsize\": %.17g, \"nodata\": %.17g, "
                 "\"xllcorner\": %.17g, \"yllcorner\": %.17g, \"dt\": %.17g, \"time0\": %.17g, \"timmax\": %.17g, "
@@ -523,7 +540,7 @@ void print_check(const Case& c, const std::vector<Event>& ev, long long iters) {
                 "\"fractions\": [%.17g, %.17g, %.17g], \"ev_wl_min\": %.17g, \"evaporation\": %d, "
                 "\"dtrain\": %.17g, \"nrain\": %zu, \"rain_total\": %.17g, \"evap_total\": %.17g, "
                 "\"dem_total\": %.17g, \"h0_total\": %.17g, \"efdc\": %d",
-                c.name.c_str(), c.grid.rows, c.grid.cols, c.grid.cellsize, c.grid.nodata, c.grid.xll, c.grid.yll,
+                json_str(c.name).c_str(), c.grid.rows, c.grid.cols, c.grid.cellsize, c.grid.nodata, c.grid.xll, c.grid.yll,
                 c.dt, c.time0, c.timmax, c.lpout, c.lkout, iters, c.manning, c.frac_int, c.frac_inf, c.frac_lwl,
                 c.ev_wl_min, c.evaporation_on, c.dtrain, c.rain.size(), [&] {
                     double s = 0;
