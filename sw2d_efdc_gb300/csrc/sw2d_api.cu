@@ -88,6 +88,7 @@ struct sw2d_handle {
     /* coupling */
     int nfaces = 0, lagged = 1;
     std::vector<int> f_side, f_i, f_j, f_cell;
+    std::vector<double> f_prev; /* FP32 handles: the previous sample's face velocities */
     int* d_face = nullptr;      /* nfaces * 2: padded cell index, side */
     double* d_face_vel = nullptr;
     double* d_face_q = nullptr;
@@ -1154,7 +1155,6 @@ int sw2d_restore(sw2d_handle* h, const void* buf, size_t bytes) {
 
 int sw2d_set_coupling_mask(sw2d_handle* h, const int* mask, int lagged, int* n_faces_out) {
     if (!h || !mask) return fail(SW2D_ERR_INVALID, "null argument");
-    if (h->fp32()) return fail(SW2D_ERR_STATE, "coupling: FP64 precision only");
     int rc = set_device(h);
     if (rc) return rc;
     const int rows = h->R, cols = h->C;
@@ -1193,6 +1193,12 @@ int sw2d_set_coupling_mask(sw2d_handle* h, const int* mask, int lagged, int* n_f
     }
     h->nfaces = (int)h->f_side.size();
     h->lagged = lagged ? 1 : 0;
+    if (h->fp32()) {
+        /* FP32 handles sample on the host from the downloaded state */
+        h->f_prev.assign((size_t)h->nfaces, 0.0);
+        if (n_faces_out) *n_faces_out = h->nfaces;
+        return SW2D_OK;
+    }
     dfree(h->d_face);
     dfree(h->d_face_vel);
     dfree(h->d_face_q);
@@ -1229,10 +1235,39 @@ void launch_couple(const StepParams& p, int nfaces, const int* faces, int lagged
                    double* q, cudaStream_t s);
 }
 
+/* Boundary-discharge sample of an FP32 handle: the k_couple rule on the
+ * host, from the state and its uua / vva (velocities_fp32). */
+static int couple_sample_fp32(sw2d_handle* h, int initial, double* q_out, int capacity) {
+    const size_t n = (size_t)h->R * h->C;
+    std::vector<double> d(n), uua(n), vva(n);
+    std::string err;
+    int rc = h->eng->get_state(h->eng_idx, d.data(), nullptr, nullptr, &err);
+    if (rc) return fail(rc, err);
+    if ((rc = velocities_fp32(h, nullptr, nullptr, uua.data(), vva.data()))) return rc;
+    const double dx = h->cfg.dx, dy = h->cfg.dy;
+    for (int k = 0; k < h->nfaces; k++) {
+        const int p = h->f_cell[k], side = h->f_side[k];
+        const double vnow = side <= 1 ? uua[p] : vva[p];
+        const double v = initial ? 0.0 : (h->lagged ? h->f_prev[k] : vnow);
+        const double hh = d[p];
+        double q;
+        switch (side) {
+        case 1: q = (v < 0) ? -v * hh * dx : 0.00; break; /* south */
+        case 0: q = (v > 0) ? v * hh * dx : 0.00; break;  /* north */
+        case 2: q = (v < 0) ? -v * hh * dy : 0.00; break; /* east */
+        default: q = (v > 0) ? v * hh * dy : 0.00; break; /* west */
+        }
+        if (q_out && k < capacity) q_out[k] = q;
+        h->f_prev[k] = vnow;
+    }
+    return SW2D_OK;
+}
+
 extern "C" int sw2d_couple_sample(sw2d_handle* h, int initial, double* q_out, int capacity) {
     int rc = check_ready(h);
     if (rc) return rc;
     if (h->nfaces == 0) return SW2D_OK;
+    if (h->fp32()) return couple_sample_fp32(h, initial, q_out, capacity);
     StepParams p = h->params();
     sw2d::launch_couple(p, h->nfaces, h->d_face, h->lagged, initial, h->d_face_vel, h->d_face_q, h->stream);
     if ((rc = sync_check(h))) return rc;

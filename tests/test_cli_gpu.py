@@ -133,3 +133,37 @@ def test_cli_fp32_form_stays_within_a_millimetre(tmp_path):
         dg = np.array(got[k:k + n_cells], float)
         de = np.array(exp[k:k + n_cells], float)
         assert np.abs(dg - de).max() < 1e-3, n
+
+
+def test_cli_fp32_coupled_case(tmp_path):
+    """--fp32 on a coupled case: the same boundary faces and cards, QSER.INP
+    discharges within 1 % of the FP64 run's largest."""
+    rng = np.random.default_rng(12)
+    R, C = 26, 22
+    dem = 30.0 - 0.12 * np.arange(R)[:, None] + 0.08 * rng.standard_normal((R, C))
+    mask = np.zeros((R, C), np.int32)
+    mask[12:20, 6:15] = 1
+    dem[mask == 1] -= 2.0
+    h0 = np.zeros((R, C))
+    h0[mask == 1] = 1.5
+    s2 = {"efdc_basetime": 3600.0, "nlayers": 2}
+    qser = {}
+    for prec in ("fp64", "fp32"):
+        root = tmp_path / prec
+        c = D.DbCase(name="lake", dem=dem, h0=h0, cellsize=8.0, dt=0.05, end=(0, 0, 0, 9), dkout=1.5, dpout=3.0,
+                     efdc=1, mask=mask, template=_template("\n", rows=2), section2=s2,
+                     rain=np.array([40.0, 40.0, 0.0]), out=(0, 0, 0, 1, 0))
+        D.write_db(root, [c])
+        args = [cli(), "--root", str(root), "--quiet"] + (["--fp32"] if prec == "fp32" else [])
+        r = subprocess.run(args, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stdout + r.stderr
+        edir = root / "db" / "lake" / "EFDC" / "input"
+        qser[prec] = (edir / "QSER.INP").read_text().splitlines()
+        assert (edir / "EFDC.INP").read_bytes() == ((tmp_path / "fp64" / "db" / "lake" / "EFDC" / "input" /
+                                                     "EFDC.INP").read_bytes())
+    a, b = qser["fp64"], qser["fp32"]
+    assert len(a) == len(b)
+    va = np.array([float(x) for l in a[14:] if not l.strip().startswith("0 ") for x in l.split()])
+    vb = np.array([float(x) for l in b[14:] if not l.strip().startswith("0 ") for x in l.split()])
+    assert va.shape == vb.shape and va.max() > 0
+    assert np.abs(va - vb).max() <= 1e-2 * va.max()

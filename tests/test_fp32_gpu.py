@@ -153,3 +153,29 @@ def test_fp32_fixed_dt_clock_follows_the_reference_time_grid():
     assert n64 == n32
     assert m32.time()[0] == m64.time()[0]
     assert np.abs(m64.depth() - m32.depth()).max() < DEPTH_TOL
+
+
+def test_fp32_coupling_samples_track_fp64():
+    """The boundary-discharge hand-off on an FP32 handle (sampled on the host
+    from the state): the same faces as FP64, the lagged samples within 1 % of
+    the largest FP64 face discharge."""
+    case = bumpy_case(R=60, C=70, seed=27, t_end=40.0, dt=0.05, holes=False, rain=np.array([30.0, 30.0, 0.0]),
+                      dtrain=3600.0)
+    mask = np.zeros(case.dem.shape, np.int32)
+    mask[25:40, 20:45] = 1
+    case.dem[mask == 1] -= 1.0
+    case.h0[mask == 1] = 1.0
+    ms = [model_from_case(case, precision=p) for p in (api.FP64, api.FP32)]
+    faces = [m.set_coupling_mask(mask, lagged=True) for m in ms]
+    assert faces[0] == faces[1] > 0
+    for a, b in zip(ms[0].coupling_faces(), ms[1].coupling_faces()):
+        assert np.array_equal(a, b)
+    qs = [[m.couple_sample(initial=True)] for m in ms]
+    for t in (10.0, 20.0, 30.0, 40.0):
+        for m, q in zip(ms, qs):
+            m.advance(t)
+            q.append(m.couple_sample())
+    q64, q32 = np.array(qs[0]), np.array(qs[1])
+    assert not q64[0].any() and not q32[0].any()
+    assert q64[1:].max() > 0
+    assert np.abs(q64 - q32).max() <= 1e-2 * q64.max()
