@@ -867,10 +867,12 @@ int sw2d_set_point_sources(sw2d_handle* h, int nsrc, const int* cells, const dou
 }
 
 int sw2d_advance(sw2d_handle* h, double t_end, int64_t* iterations_out) {
+    sw2d::NvtxRange r("sw2d_advance");
     return run_until(h, t_end, -1, iterations_out);
 }
 
 int sw2d_step(sw2d_handle* h, int n, double t_end) {
+    sw2d::NvtxRange r("sw2d_step");
     if (n < 0) return fail(SW2D_ERR_INVALID, "n < 0");
     int64_t done = 0;
     if (h && !h->fp32() && h->cfg.dt_mode == SW2D_DT_CFL && (n & 1)) {
@@ -1089,22 +1091,61 @@ int sw2d_get_timing(sw2d_handle* h, double* ms, double* kernel_ms, int* nk) {
     return SW2D_OK;
 }
 
+/* snapshot layout: a 64-byte header (magic, rows, cols, pitch, clock size),
+ * the device clock, then the state arrays: FP64 h, qx, qy (padded); FP32 h,
+ * qx, qy and the Kahan compensation (padded binary32) */
+constexpr int64_t kSnapMagic64 = 0x53573244534e4150LL, kSnapMagic32 = 0x5357324433325350LL;
+
 int sw2d_snapshot_size(sw2d_handle* h, size_t* bytes) {
     if (!h || !bytes) return fail(SW2D_ERR_INVALID, "null argument");
-    if (h->fp32()) return fail(SW2D_ERR_STATE, "snapshot: FP64 precision only");
+    if (h->fp32()) {
+        if (h->eng_idx < 0) return fail(SW2D_ERR_STATE, "set_depth first");
+        *bytes = 64 + h->eng->snapshot_bytes(h->eng_idx);
+        return SW2D_OK;
+    }
     *bytes = 64 + sizeof(DevClock) + 3 * h->ncell * sizeof(double);
+    return SW2D_OK;
+}
+
+static int snapshot_fp32(sw2d_handle* h, void* buf, size_t bytes) {
+    size_t need;
+    int rc = sw2d_snapshot_size(h, &need);
+    if (rc) return rc;
+    if (!buf || bytes < need) return fail(SW2D_ERR_INVALID, "snapshot buffer too small");
+    const sw2d::Scenario32& S = h->eng->at(h->eng_idx);
+    int64_t hdr[8] = {kSnapMagic32, h->R, h->C, S.P, (int64_t)sizeof(sw2d::Clock32), 0, 0, 0};
+    std::memcpy(buf, hdr, 64);
+    std::string err;
+    if ((rc = h->eng->snapshot(h->eng_idx, (char*)buf + 64, &err))) return fail(rc, err);
+    return SW2D_OK;
+}
+
+static int restore_fp32(sw2d_handle* h, const void* buf, size_t bytes) {
+    if (h->eng_idx < 0) return fail(SW2D_ERR_STATE, "set_depth first");
+    size_t need;
+    int rc = sw2d_snapshot_size(h, &need);
+    if (rc) return rc;
+    if (bytes < need) return fail(SW2D_ERR_INVALID, "snapshot too small");
+    const sw2d::Scenario32& S = h->eng->at(h->eng_idx);
+    int64_t hdr[8];
+    std::memcpy(hdr, buf, 64);
+    if (hdr[0] != kSnapMagic32 || hdr[1] != h->R || hdr[2] != h->C || hdr[3] != S.P ||
+        hdr[4] != (int64_t)sizeof(sw2d::Clock32))
+        return fail(SW2D_ERR_INVALID, "snapshot does not match this model");
+    std::string err;
+    if ((rc = h->eng->restore(h->eng_idx, (const char*)buf + 64, &err))) return fail(rc, err);
     return SW2D_OK;
 }
 
 int sw2d_snapshot(sw2d_handle* h, void* buf, size_t bytes) {
     int rc = check_ready(h);
     if (rc) return rc;
-    if (h->fp32()) return fail(SW2D_ERR_STATE, "snapshot: FP64 precision only");
+    if (h->fp32()) return snapshot_fp32(h, buf, bytes);
     size_t need;
     sw2d_snapshot_size(h, &need);
     if (!buf || bytes < need) return fail(SW2D_ERR_INVALID, "snapshot buffer too small");
     char* p = (char*)buf;
-    int64_t hdr[8] = {0x53573244534e4150LL, h->R, h->C, h->P, (int64_t)sizeof(DevClock), 0, 0, 0};
+    int64_t hdr[8] = {kSnapMagic64, h->R, h->C, h->P, (int64_t)sizeof(DevClock), 0, 0, 0};
     std::memcpy(p, hdr, 64);
     p += 64;
     CK(cudaMemcpy(p, h->clk, sizeof(DevClock), cudaMemcpyDeviceToHost));
@@ -1119,8 +1160,11 @@ int sw2d_snapshot(sw2d_handle* h, void* buf, size_t bytes) {
 
 int sw2d_restore(sw2d_handle* h, const void* buf, size_t bytes) {
     if (!h || !buf) return fail(SW2D_ERR_INVALID, "null argument");
-    if (h->fp32()) return fail(SW2D_ERR_STATE, "restore: FP64 precision only");
     if (!h->have_dem) return fail(SW2D_ERR_STATE, "set_dem first");
+    if (h->fp32()) {
+        int rc = set_device(h);
+        return rc ? rc : restore_fp32(h, buf, bytes);
+    }
     int rc = set_device(h);
     if (rc) return rc;
     size_t need;
@@ -1129,7 +1173,7 @@ int sw2d_restore(sw2d_handle* h, const void* buf, size_t bytes) {
     const char* p = (const char*)buf;
     int64_t hdr[8];
     std::memcpy(hdr, p, 64);
-    if (hdr[0] != 0x53573244534e4150LL || hdr[1] != h->R || hdr[2] != h->C || hdr[3] != h->P ||
+    if (hdr[0] != kSnapMagic64 || hdr[1] != h->R || hdr[2] != h->C || hdr[3] != h->P ||
         hdr[4] != (int64_t)sizeof(DevClock))
         return fail(SW2D_ERR_INVALID, "snapshot does not match this model");
     p += 64;
@@ -1264,6 +1308,7 @@ static int couple_sample_fp32(sw2d_handle* h, int initial, double* q_out, int ca
 }
 
 extern "C" int sw2d_couple_sample(sw2d_handle* h, int initial, double* q_out, int capacity) {
+    sw2d::NvtxRange r("sw2d_couple_sample");
     int rc = check_ready(h);
     if (rc) return rc;
     if (h->nfaces == 0) return SW2D_OK;

@@ -225,6 +225,7 @@ int sw2d_batch_submit(sw2d_batch* b, const sw2d_scenario* s, int64_t* id_out) {
 }
 
 int sw2d_batch_step(sw2d_batch* b, int iterations, int* n_running_out, int* n_queued_out) {
+    sw2d::NvtxRange r("sw2d_batch_step");
     if (!b || iterations < 0) return bfail(SW2D_ERR_INVALID, "invalid argument");
     if (cudaSetDevice(b->device) != cudaSuccess) return bfail(SW2D_ERR_CUDA, "cudaSetDevice");
     std::string err;

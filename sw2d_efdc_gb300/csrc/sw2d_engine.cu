@@ -568,6 +568,50 @@ int Engine32::get_state(int index, double* depth, double* qx, double* qy, std::s
     return SW2D_OK;
 }
 
+size_t Engine32::snapshot_bytes(int index) const {
+    const Scenario32& S = *scn_[index];
+    return sizeof(Clock32) + 4 * (size_t)S.P * S.NR * sizeof(float);
+}
+
+int Engine32::snapshot(int index, void* buf, std::string* err) {
+    Scenario32& S = *scn_[index];
+    Clock32 c;
+    int rc = get_clock(index, &c, err);
+    if (rc) return rc;
+    char* p = static_cast<char*>(buf);
+    std::memcpy(p, &c, sizeof c);
+    p += sizeof c;
+    const size_t n = (size_t)S.P * S.NR * sizeof(float);
+    const float* src[4] = {S.d.h[c.slot.cur], S.d.qx[c.slot.cur], S.d.qy[c.slot.cur], S.d.kc};
+    for (int k = 0; k < 4; k++) {
+        ECK(cudaMemcpyAsync(p, src[k], n, cudaMemcpyDeviceToHost, stream_));
+        p += n;
+    }
+    ECK(cudaStreamSynchronize(stream_));
+    return SW2D_OK;
+}
+
+int Engine32::restore(int index, const void* buf, std::string* err) {
+    Scenario32& S = *scn_[index];
+    const char* p = static_cast<const char*>(buf);
+    Clock32 c;
+    std::memcpy(&c, p, sizeof c);
+    p += sizeof c;
+    if (c.slot.cur != 0 && c.slot.cur != 1) {
+        if (err) *err = "snapshot clock is not valid";
+        return SW2D_ERR_INVALID;
+    }
+    const size_t n = (size_t)S.P * S.NR * sizeof(float);
+    float* dst[4] = {S.d.h[c.slot.cur], S.d.qx[c.slot.cur], S.d.qy[c.slot.cur], S.d.kc};
+    for (int k = 0; k < 4; k++) {
+        ECK(cudaMemcpyAsync(dst[k], p, n, cudaMemcpyHostToDevice, stream_));
+        p += n;
+    }
+    ECK(cudaMemcpyAsync(S.d.clk, &c, sizeof c, cudaMemcpyHostToDevice, stream_));
+    ECK(cudaStreamSynchronize(stream_));
+    return SW2D_OK;
+}
+
 int Engine32::get_volume(int index, double* vol, double* smax, std::string* err) {
     int rc = rebuild(err);
     if (rc) return rc;

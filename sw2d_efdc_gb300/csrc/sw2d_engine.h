@@ -7,12 +7,23 @@
 #include "sw2d.h"
 #include "sw2d_fp32.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <map>
 #include <memory>
 #include <string>
 #include <vector>
 
 namespace sw2d {
+
+/* A named range on the NVTX timeline around a host call (free when no
+ * profiler is attached). */
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 struct ScenarioInput {
     int rows = 0, cols = 0;
@@ -69,6 +80,12 @@ class Engine32 {
     int get_clock(int index, Clock32* out, std::string* err);
     int get_volume(int index, double* vol, double* smax, std::string* err);
     int get_outlet(int index, double* t, double* q, int cap, int* count, std::string* err);
+    /* the scenario's device state (clock, then depth, x and y discharges and
+     * the Kahan compensation, whole padded arrays) to / from a host buffer of
+     * snapshot_bytes(index) bytes */
+    size_t snapshot_bytes(int index) const;
+    int snapshot(int index, void* buf, std::string* err);
+    int restore(int index, const void* buf, std::string* err);
     cudaStream_t stream() const { return stream_; }
     size_t bytes_in_use() const;
     double last_ms() const { return last_ms_; }

@@ -179,3 +179,30 @@ def test_fp32_coupling_samples_track_fp64():
     assert not q64[0].any() and not q32[0].any()
     assert q64[1:].max() > 0
     assert np.abs(q64 - q32).max() <= 1e-2 * q64.max()
+
+
+def test_fp32_snapshot_restore_is_exact():
+    """Checkpoint and resume of an FP32 handle (depth, discharges, Kahan
+    compensation, clock and ledger): the resumed run is bit-identical, also
+    in a second handle of the same raster; a snapshot of another raster or
+    precision is refused."""
+    case = bumpy_case(R=90, C=240, seed=28, dt_mode=O.DT_CFL, cfl=0.7, dt_max=1.5, outflow_south=True,
+                      rain=np.array([12.0, 12.0, 0.0]), dtrain=60.0, t_end=1e9, holes=True)
+    m = model_from_case(case, precision=api.FP32)
+    m.step(30)
+    snap = m.snapshot()
+    m.step(40)
+    h_a, l_a = m.depth(), m.ledger()
+    m.restore(snap)
+    m.step(40)
+    assert np.array_equal(m.depth(), h_a) and m.ledger() == l_a
+    m2 = model_from_case(case, precision=api.FP32)
+    m2.restore(snap)
+    m2.step(40)
+    assert np.array_equal(m2.depth(), h_a) and m2.ledger()["time"] == l_a["time"]
+    other = model_from_case(bumpy_case(R=90, C=241, seed=28, holes=False), precision=api.FP32)
+    with pytest.raises(api.Sw2dError):
+        other.restore(snap)
+    m64 = model_from_case(case, precision=api.FP64)
+    with pytest.raises(api.Sw2dError):
+        m64.restore(snap)
