@@ -252,12 +252,22 @@ std::string lines(const char* const* l, size_t n) {
 
 std::string format(const char* fmt, ...) __attribute__((format(printf, 1, 2)));
 std::string format(const char* fmt, ...) {
-    char buf[512];
-    va_list ap;
+    va_list ap, aq;
     va_start(ap, fmt);
+    va_copy(aq, ap);
+    char buf[512];
     const int n = std::vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
-    return std::string(buf, n < 0 ? 0 : std::min<size_t>((size_t)n, sizeof buf - 1));
+    std::string out;
+    if (n >= (int)sizeof buf) { /* a longer line: format it again at its length */
+        out.resize((size_t)n + 1);
+        std::vsnprintf(&out[0], out.size(), fmt, aq);
+        out.resize((size_t)n);
+    } else if (n > 0) {
+        out.assign(buf, (size_t)n);
+    }
+    va_end(aq);
+    return out;
 }
 
 } // namespace
