@@ -25,8 +25,10 @@ OUTFLOW_NONE, OUTFLOW_SOUTH = 0, 1
 STATUS = {
     0: "ok", -1: "invalid argument", -2: "CUDA error", -3: "out of memory", -4: "invalid state",
     -5: "HBM budget exceeded", -6: "non-finite state", -7: "no sm_103 device", -8: "timeout",
-    -9: "not found",
+    -9: "not found", -10: "file error",
 }
+(SW2D_OK, SW2D_ERR_INVALID, SW2D_ERR_CUDA, SW2D_ERR_NOMEM, SW2D_ERR_STATE, SW2D_ERR_BUDGET, SW2D_ERR_NUMERIC,
+ SW2D_ERR_NODEVICE, SW2D_ERR_TIMEOUT, SW2D_ERR_NOT_FOUND, SW2D_ERR_IO) = range(0, -11, -1)
 
 
 class Sw2dError(RuntimeError):
@@ -129,6 +131,7 @@ SIGNATURES = {
     "sw2d_write_qser": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip, C.c_int, _dp, _dp]),
     "sw2d_write_efdc_cards": (C.c_int, [C.c_char_p, C.c_int, _ip, _ip, _ip, C.c_int, C.c_int, C.c_int]),
     "sw2d_lake_catchment_smooth": (C.c_int, [C.c_int, C.c_int, _ip, _dp]),
+    "sw2d_test_stall_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "sw2d_evaporation_series": (C.c_int, [C.c_int, _dp, _dp, C.c_double, C.c_double, _dp]),
     "sw2d_measure_state_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
@@ -320,6 +323,11 @@ class Model:
         _check(load().sw2d_couple_sample(self._h, int(bool(initial)), _ptr(q, _dp), self._nfaces),
                "sw2d_couple_sample")
         return q
+
+    def stall_staging(self, on=True):
+        """Failure-test hook (FP32): the kernel issues no staged loads, so its
+        bounded wait runs out and the next step fails with SW2D_ERR_TIMEOUT."""
+        _check(load().sw2d_test_stall_staging(self._h, int(bool(on))), "sw2d_test_stall_staging")
 
     def snapshot(self) -> bytes:
         n = C.c_size_t(0)

@@ -55,7 +55,7 @@ def _compile(unit: str) -> tuple[str, str]:
     src = os.path.join(CSRC, unit)
     obj = os.path.join(OBJ_DIR, unit.replace(".cu", ".o"))
     deps = [src, os.path.join(ROOT, "include", "sw2d.h"), os.path.join(ROOT, "include", "sw2d_batch.h"),
-                  os.path.join(ROOT, "include", "sw2d_noalloc.h")] + \
+                  os.path.join(ROOT, "include", "sw2d_noalloc.h"), os.path.join(ROOT, "include", "sw2d_test.h")] + \
         [os.path.join(CSRC, h) for h in HEADERS]
     if not _stale(obj, deps + [__file__]):
         return obj, ""

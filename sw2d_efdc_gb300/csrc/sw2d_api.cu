@@ -9,6 +9,7 @@
  */
 #include "sw2d.h"
 #include "sw2d_engine.h"
+#include "sw2d_test.h"
 #include "sw2d_internal.h"
 
 #include <cuda_runtime.h>
@@ -1193,6 +1194,14 @@ int sw2d_restore(sw2d_handle* h, const void* buf, size_t bytes) {
     fp64_launch_face_velocity(sp, 0, h->stream);
     if ((rc = sync_check(h))) return rc;
     return prime(h, 0);
+}
+
+int sw2d_test_stall_staging(sw2d_handle* h, int on) {
+    if (!h) return fail(SW2D_ERR_INVALID, "null handle");
+    if (!h->fp32()) return fail(SW2D_ERR_STATE, "staging stall: FP32 handles only");
+    if (h->eng_idx < 0) return fail(SW2D_ERR_STATE, "set_depth first");
+    h->eng->set_stall_staging(h->eng_idx, on != 0);
+    return SW2D_OK;
 }
 
 /* ---------------- coupling: SW2D-EFDC.cu:728-1067 ---------------------- */

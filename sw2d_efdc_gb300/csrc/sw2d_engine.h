@@ -83,6 +83,12 @@ class Engine32 {
     /* the scenario's device state (clock, then depth, x and y discharges and
      * the Kahan compensation, whole padded arrays) to / from a host buffer of
      * snapshot_bytes(index) bytes */
+    /* failure test: the scenario's work items issue no staged loads, so the
+     * kernel's bounded wait gives up and sets the timeout status bit */
+    void set_stall_staging(int index, bool on) {
+        scn_[index]->d.stall_staging = on ? 1 : 0;
+        dirty_ = true;
+    }
     size_t snapshot_bytes(int index) const;
     int snapshot(int index, void* buf, std::string* err);
     int restore(int index, const void* buf, std::string* err);

@@ -345,7 +345,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         if (has_cls) tma_load_2d(&S.cls[st].v[0][0], &P.tm_cls, c0, y - 2, &S.bar[st]);
         if (has_rw) tma_load_2d(&S.rw[st].v[0][0], &P.tm_rw, c0, y - 3, &S.bar[st]);
     };
-    if (tid == 0)
+    if (tid == 0 && !P.stall_staging)
         for (int b = 0; b < NS && b < nblk; b++) issue(b, b);
 
     /* lane geometry: staged columns sc, sc+1; global columns cg, cg+1 */

@@ -92,6 +92,7 @@ struct Scn32 {
     int outflow_south, ledger_cells, series_mode, dt_mode;
     int nrain, nevap, outlet_cap;
     int nsrc, nq;
+    int stall_staging;     /* failure test: issue no staged loads, so the bounded wait runs out */
     double dtoq;
     float dx, dy, rdx, rdy, th, g;
     float pct_lake, pct_land, ev_wl_min;
