@@ -5,6 +5,8 @@
   reduction is independent of the rest of the batch).
 * Admission respects the HBM budget and the queue drains as scenarios finish.
 * A batch scenario equals the same scenario run through a single FP32 handle.
+* Cancelling a running request frees its slot for a queued one and leaves
+  the other requests' results unchanged.
 """
 import numpy as np
 import pytest
@@ -85,3 +87,32 @@ def test_batch_equals_single_fp32_handle():
     m.advance(80.0)
     h, qx, qy = m.state()
     assert np.array_equal(h, res[0][0]) and np.array_equal(qx, res[0][1])
+
+
+def test_cancel_mid_run_frees_the_slot_and_leaves_the_others_unchanged():
+    """Releasing a running request cancels it between steps: its memory goes
+    back to the budget, a queued request is admitted in its place, and the
+    other requests finish exactly as they would alone."""
+    a, b_, c = scenario(128, 21, 60.0), scenario(128, 22, 60.0), scenario(128, 23, 60.0)
+    alone = {k: run_batch([s])[0][0] for k, s in (("a", a), ("c", c))}
+    bt = api.Batch(hbm_budget_bytes=2.5 * 128 * 136 * 40)
+    ia, ib, ic = (bt.submit(**s) for s in (a, b_, c))
+    nr, nq = bt.step(8)
+    assert (nr, nq) == (2, 1)
+    assert bt.poll(ib)[0] == api.REQ_RUNNING
+    bt.release(ib)
+    with pytest.raises(api.Sw2dError) as e:
+        bt.poll(ib)
+    assert e.value.code == api.SW2D_ERR_NOT_FOUND
+    for _ in range(10000):
+        nr, nq = bt.step(32)
+        if nr == 0 and nq == 0:
+            break
+    for k, i in (("a", ia), ("c", ic)):
+        st, led = bt.poll(i)
+        assert st == api.REQ_DONE
+        (h0, qx0, qy0), l0 = alone[k]
+        h1, qx1, qy1 = bt.result(i)
+        assert np.array_equal(h0, h1) and np.array_equal(qx0, qx1) and np.array_equal(qy0, qy1)
+        assert led["time"] == l0["time"] == 60.0
+    bt.close()
