@@ -41,6 +41,10 @@ BYTES_PER_CELL_K64_FLUX = 66
 # (profiles/k64_flux_4096.md)
 TRAFFIC_PER_CELL_K64_FLUX = 63.93
 BYTES_PER_CELL_FP32_CFG3 = 37  # h,qx,qy r+w 24 + z offset 4 + info byte 1 + Kahan compensation r+w 8
+# DRAM bytes per cell of one k32_march launch, 4096 x 4096 precision form at t = 1200 s: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum = 360.3 + 221.8 MB over 16.78 M cells
+# (profiles/k32_march_4096.md); the launch streams every field once, so the figure scales with cells
+TRAFFIC_PER_CELL_K32_MARCH = 34.69
 
 
 class TimedRegion:
@@ -254,7 +258,8 @@ def run_fp32_leg(args, peak):
         "roofline": {"bound": "hbm", "kernel": "k32_march + k32_finalize",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3,
-                     "traffic": None},
+                     "traffic": round(TRAFFIC_PER_CELL_K32_MARCH * cells / 1e9, 4),
+                     "traffic_unit": "GB per launch (ncu at 4096x4096, scaled by cells)"},
         "balance_error": led["balance_error"],
         "vs_fp64_plain": None,
     }
