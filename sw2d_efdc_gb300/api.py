@@ -329,16 +329,22 @@ class Model:
         bounded wait runs out and the next step fails with SW2D_ERR_TIMEOUT."""
         _check(load().sw2d_test_stall_staging(self._h, int(bool(on))), "sw2d_test_stall_staging")
 
-    def snapshot(self) -> bytes:
+    def snapshot(self) -> bytearray:
+        """The device state as a host buffer (written in place, no extra copy)."""
         n = C.c_size_t(0)
         _check(load().sw2d_snapshot_size(self._h, C.byref(n)), "sw2d_snapshot_size")
-        buf = C.create_string_buffer(n.value)
-        _check(load().sw2d_snapshot(self._h, buf, n.value), "sw2d_snapshot")
-        return buf.raw
+        buf = bytearray(n.value)
+        _check(load().sw2d_snapshot(self._h, (C.c_char * n.value).from_buffer(buf), n.value), "sw2d_snapshot")
+        return buf
 
-    def restore(self, data: bytes):
-        buf = C.create_string_buffer(data, len(data))
-        _check(load().sw2d_restore(self._h, buf, len(data)), "sw2d_restore")
+    def restore(self, data):
+        """Restore a snapshot (bytes or bytearray; read in place)."""
+        if isinstance(data, bytearray):
+            ptr = (C.c_char * len(data)).from_buffer(data)
+        else:
+            data = bytes(data)
+            ptr = C.c_char_p(data)
+        _check(load().sw2d_restore(self._h, ptr, len(data)), "sw2d_restore")
 
     def set_profiling(self, on=True):
         _check(load().sw2d_set_profiling(self._h, int(bool(on))), "sw2d_set_profiling")

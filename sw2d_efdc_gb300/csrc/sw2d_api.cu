@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -82,7 +83,8 @@ struct sw2d_handle {
     /* host mirrors */
     std::vector<uint8_t> host_flags;
     std::vector<float> host_rainw;
-    double active_weight = 0.0; /* sum over active cells of the rain weight */
+    mutable double active_weight = 0.0; /* sum over active cells of the rain weight */
+    mutable bool aw_dirty = false;      /* recomputed when the next launch's parameters are built */
     bool have_dem = false, have_depth = false;
     int nrain = 0, nevap = 0, nsrc = 0, nq = 0, outlet_cap = 0;
     double dtrain = 3600.0, dtoq = 3600.0;
@@ -90,6 +92,8 @@ struct sw2d_handle {
     int nfaces = 0, lagged = 1;
     std::vector<int> f_side, f_i, f_j, f_cell;
     std::vector<double> f_prev; /* FP32 handles: the previous sample's face velocities */
+    void* pin = nullptr;        /* pinned staging of large device-to-host copies */
+    size_t pin_bytes = 0;
     int* d_face = nullptr;      /* nfaces * 2: padded cell index, side */
     double* d_face_vel = nullptr;
     double* d_face_q = nullptr;
@@ -132,6 +136,7 @@ struct sw2d_handle {
         p.pct_lake = 1.00 - cfg.frac_lwl;                  /* SW2D-EFDC.cu:627 */
         p.pct_land = 1.00 - (cfg.frac_int + cfg.frac_inf); /* SW2D-EFDC.cu:631 */
         p.ledger_cells = (p.pct_lake != p.pct_land) || (nevap > 0);
+        if (aw_dirty) update_active_weight();
         p.rain_static = active_weight * p.pct_land;
         p.dx = cfg.dx;
         p.dy = cfg.dy;
@@ -184,13 +189,14 @@ struct sw2d_handle {
 
     size_t pad_index(int r, int c) const { return (size_t)(r + SW2D_HALO) * P + (c + SW2D_HALO); }
 
-    void update_active_weight() {
+    void update_active_weight() const {
         double s = 0.0;
         for (int r = 0; r < R; r++)
             for (int c = 0; c < C; c++)
                 if (host_flags[pad_index(r, c)] & SW2D_F_ACTIVE)
                     s += host_rainw.empty() ? 1.0 : (double)host_rainw[(size_t)r * C + c];
         active_weight = s;
+        aw_dirty = false;
     }
 };
 
@@ -214,25 +220,119 @@ void dfree(T*& p) {
     p = nullptr;
 }
 
-/* Copy a rows x cols host raster into the interior of a padded device field. */
+/* Large device-to-host copies go through a pinned staging buffer and a
+ * multithreaded host copy: a copy straight into pageable memory runs at a
+ * few GB/s (the driver bounces it through its own pinned chunks, one at a
+ * time, faulting the destination's fresh pages in as it goes), while a copy
+ * into pinned memory runs at the host link's rate. */
+constexpr size_t kStageMin = (size_t)4 << 20;
+
+int stage_reserve(sw2d_handle* h, size_t bytes) {
+    if (h->pin_bytes >= bytes) return SW2D_OK;
+    if (h->pin) cudaFreeHost(h->pin);
+    h->pin = nullptr;
+    h->pin_bytes = 0;
+    CK(cudaMallocHost(&h->pin, bytes));
+    h->pin_bytes = bytes;
+    return SW2D_OK;
+}
+
+/* f(first, last) over [0, n) split across up to 16 host threads */
+template <typename F>
+void parallel_ranges(size_t n, F f) {
+    const size_t nt = std::max<size_t>(1, std::min<size_t>({16, std::thread::hardware_concurrency(), n / 8 + 1}));
+    if (nt == 1) {
+        f((size_t)0, n);
+        return;
+    }
+    std::vector<std::thread> th;
+    const size_t per = (n + nt - 1) / nt;
+    for (size_t t = 0; t < nt; t++) {
+        const size_t a = t * per, b = std::min(n, a + per);
+        if (a < b) th.emplace_back([=] { f(a, b); });
+    }
+    for (auto& x : th) x.join();
+}
+
+int d2h(sw2d_handle* h, void* dst, const void* src, size_t bytes) {
+    if (bytes < kStageMin) {
+        CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return SW2D_OK;
+    }
+    int rc = stage_reserve(h, bytes);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->pin, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    const char* s = static_cast<const char*>(h->pin);
+    char* d = static_cast<char*>(dst);
+    const size_t chunk = (size_t)1 << 20;
+    parallel_ranges((bytes + chunk - 1) / chunk, [&](size_t a, size_t b) {
+        for (size_t k = a; k < b; k++) std::memcpy(d + k * chunk, s + k * chunk, std::min(chunk, bytes - k * chunk));
+    });
+    return SW2D_OK;
+}
+
+/* Copy a rows x cols host raster into the interior of a padded device field
+ * (large rasters: rows laid out with the field's pitch in the pinned staging
+ * buffer by host threads, then one copy). */
 template <typename T>
 int upload_interior(sw2d_handle* h, T* dst, const T* src, int rows, int cols) {
-    CK(cudaMemcpy2DAsync(dst + h->pad_index(0, 0), (size_t)h->P * sizeof(T), src, (size_t)cols * sizeof(T),
-                         (size_t)cols * sizeof(T), rows, cudaMemcpyHostToDevice, h->stream));
+    const size_t rowb = (size_t)h->P * sizeof(T);
+    if ((size_t)rows * cols * sizeof(T) < kStageMin) {
+        CK(cudaMemcpy2DAsync(dst + h->pad_index(0, 0), rowb, src, (size_t)cols * sizeof(T),
+                             (size_t)cols * sizeof(T), rows, cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return SW2D_OK;
+    }
+    int rc = stage_reserve(h, (size_t)rows * rowb);
+    if (rc) return rc;
+    T* s = static_cast<T*>(h->pin);
+    const size_t P = (size_t)h->P;
+    parallel_ranges((size_t)rows, [&](size_t a, size_t b) {
+        for (size_t r = a; r < b; r++) std::memcpy(s + r * P, src + r * cols, (size_t)cols * sizeof(T));
+    });
+    /* the staged rows' pitch columns outside the interior are not copied */
+    CK(cudaMemcpy2DAsync(dst + h->pad_index(0, 0), rowb, s, rowb, (size_t)cols * sizeof(T), rows,
+                         cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return SW2D_OK;
 }
 
 template <typename T>
 int download_block(sw2d_handle* h, T* dst, const T* src_padded, int r0, int c0, int rows, int cols) {
-    CK(cudaMemcpy2DAsync(dst, (size_t)cols * sizeof(T), src_padded + h->pad_index(r0, c0),
-                         (size_t)h->P * sizeof(T), (size_t)cols * sizeof(T), rows, cudaMemcpyDeviceToHost,
-                         h->stream));
+    const size_t rowb = (size_t)h->P * sizeof(T);
+    if ((size_t)rows * cols * sizeof(T) < kStageMin) {
+        CK(cudaMemcpy2DAsync(dst, (size_t)cols * sizeof(T), src_padded + h->pad_index(r0, c0), rowb,
+                             (size_t)cols * sizeof(T), rows, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return SW2D_OK;
+    }
+    /* whole padded rows into the staging buffer, then the interior columns out */
+    int rc = stage_reserve(h, (size_t)rows * rowb);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(h->pin, src_padded + (size_t)(r0 + SW2D_HALO) * h->P, (size_t)rows * rowb,
+                       cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
+    const T* s = static_cast<const T*>(h->pin) + (c0 + SW2D_HALO);
+    const size_t P = (size_t)h->P;
+    parallel_ranges((size_t)rows, [&](size_t a, size_t b) {
+        for (size_t r = a; r < b; r++) std::memcpy(dst + r * cols, s + r * P, (size_t)cols * sizeof(T));
+    });
     return SW2D_OK;
 }
 
 int put(sw2d_handle* h, void* dst, const void* src, size_t bytes) {
+    if (bytes >= kStageMin && stage_reserve(h, bytes) == SW2D_OK) {
+        const char* sp = static_cast<const char*>(src);
+        char* d = static_cast<char*>(h->pin);
+        const size_t chunk = (size_t)1 << 20;
+        parallel_ranges((bytes + chunk - 1) / chunk, [&](size_t a, size_t b) {
+            for (size_t k = a; k < b; k++)
+                std::memcpy(d + k * chunk, sp + k * chunk, std::min(chunk, bytes - k * chunk));
+        });
+        src = h->pin;
+    }
     CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return SW2D_OK;
@@ -608,6 +708,7 @@ int sw2d_destroy(sw2d_handle* h) {
     if (!h) return SW2D_OK;
     if (h->fp32()) {
         h->eng.reset();
+        if (h->pin) cudaFreeHost(h->pin);
         delete h;
         return SW2D_OK;
     }
@@ -645,6 +746,7 @@ int sw2d_destroy(sw2d_handle* h) {
     for (int k = 0; k < 8; k++)
         if (h->kev[k]) cudaEventDestroy(h->kev[k]);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->pin) cudaFreeHost(h->pin);
     delete h;
     return SW2D_OK;
 }
@@ -660,16 +762,18 @@ int sw2d_set_dem(sw2d_handle* h, const double* zin) {
     if (rc) return rc;
     if ((rc = upload_interior(h, h->z, zin, h->R, h->C))) return rc;
     std::fill(h->host_flags.begin(), h->host_flags.end(), 0);
-    for (int r = 0; r < h->R; r++)
-        for (int c = 0; c < h->C; c++) {
-            double v = zin[(size_t)r * h->C + c];
-            h->host_flags[h->pad_index(r, c)] = (v != h->cfg.nodata) ? SW2D_F_ACTIVE : 0; /* :37-42 */
-        }
+    parallel_ranges((size_t)h->R, [&](size_t a, size_t b) {
+        for (size_t r = a; r < b; r++)
+            for (int c = 0; c < h->C; c++) {
+                const double v = zin[r * h->C + c];
+                h->host_flags[h->pad_index((int)r, c)] = (v != h->cfg.nodata) ? SW2D_F_ACTIVE : 0; /* :37-42 */
+            }
+    });
     for (int k = 0; k < h->nsrc; k++) {
         /* source flags are re-applied by set_point_sources */
     }
     if ((rc = put(h, h->flags, h->host_flags.data(), h->ncell))) return rc;
-    h->update_active_weight();
+    h->aw_dirty = true;
     h->have_dem = true;
     h->graph_dirty = true;
     return SW2D_OK;
@@ -797,7 +901,7 @@ int sw2d_set_rain_field(sw2d_handle* h, const float* w) {
         if ((rc = upload_interior(h, h->rainw, w, h->R, h->C))) return rc;
         h->host_rainw.assign(w, w + (size_t)h->R * h->C);
     }
-    h->update_active_weight();
+    h->aw_dirty = true;
     h->graph_dirty = true;
     return SW2D_OK;
 }
@@ -964,7 +1068,7 @@ static int velocities(sw2d_handle* h, double* uu, double* vv, double* uua, doubl
     if ((rc = sync_check(h))) return rc;
     double* outs[4] = {uu, vv, uua, vva};
     for (int k = 0; k < 4; k++)
-        if (outs[k]) CK(cudaMemcpy(outs[k], h->scratch + k * n, n * sizeof(double), cudaMemcpyDeviceToHost));
+        if (outs[k] && (rc = d2h(h, outs[k], h->scratch + k * n, n * sizeof(double)))) return rc;
     return SW2D_OK;
 }
 
@@ -1153,7 +1257,7 @@ int sw2d_snapshot(sw2d_handle* h, void* buf, size_t bytes) {
     p += sizeof(DevClock);
     double* src[3] = {h->h[0], h->qx[0], h->qy[0]};
     for (int k = 0; k < 3; k++) {
-        CK(cudaMemcpy(p, src[k], h->ncell * sizeof(double), cudaMemcpyDeviceToHost));
+        if ((rc = d2h(h, p, src[k], h->ncell * sizeof(double)))) return rc;
         p += h->ncell * sizeof(double);
     }
     return SW2D_OK;

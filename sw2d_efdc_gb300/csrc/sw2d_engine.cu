@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 #include <limits>
 
 namespace sw2d {
@@ -70,6 +71,7 @@ Engine32::~Engine32() {
     if (ev_a_) cudaEventDestroy(ev_a_);
     if (ev_b_) cudaEventDestroy(ev_b_);
     if (stream_) cudaStreamDestroy(stream_);
+    if (pin_) cudaFreeHost(pin_);
 }
 
 int Engine32::init(std::string* err) {
@@ -554,12 +556,34 @@ int Engine32::get_state(int index, double* depth, double* qx, double* qy, std::s
     if (rc) return rc;
     const int cur = c.slot.cur;
     const int R = S.R, C = S.C, P = S.P;
-    std::vector<float> buf((size_t)(R + 1) * (C + 1));
+    /* whole padded rows into pinned staging (a copy into pageable memory runs
+     * at a few GB/s), then the interior widened to binary64 on host threads */
+    const size_t need = (size_t)(R + 1) * P * sizeof(float);
+    if (pin_bytes_ < need) {
+        if (pin_) cudaFreeHost(pin_);
+        pin_ = nullptr;
+        pin_bytes_ = 0;
+        ECK(cudaMallocHost(&pin_, need));
+        pin_bytes_ = need;
+    }
     auto fetch = [&](const float* src, int rows, int cols, double* dst) -> int {
-        ECK(cudaMemcpy2DAsync(buf.data(), (size_t)cols * 4, src + (size_t)M_H * P + M_H, (size_t)P * 4,
-                              (size_t)cols * 4, rows, cudaMemcpyDeviceToHost, stream_));
+        ECK(cudaMemcpyAsync(pin_, src + (size_t)M_H * P, (size_t)rows * P * sizeof(float), cudaMemcpyDeviceToHost,
+                            stream_));
         ECK(cudaStreamSynchronize(stream_));
-        for (size_t k = 0; k < (size_t)rows * cols; k++) dst[k] = buf[k];
+        const float* s = static_cast<const float*>(pin_) + M_H;
+        const size_t nt = std::max<size_t>(1, std::min<size_t>({16, std::thread::hardware_concurrency(),
+                                                                (size_t)rows / 64 + 1}));
+        std::vector<std::thread> th;
+        const size_t per = ((size_t)rows + nt - 1) / nt;
+        for (size_t t = 0; t < nt; t++) {
+            const size_t a = t * per, b = std::min((size_t)rows, a + per);
+            if (a >= b) continue;
+            th.emplace_back([=] {
+                for (size_t r = a; r < b; r++)
+                    for (int k = 0; k < cols; k++) dst[r * cols + k] = s[r * P + k];
+            });
+        }
+        for (auto& x : th) x.join();
         return SW2D_OK;
     };
     if (depth && (rc = fetch(S.d.h[cur], R, C, depth))) return rc;

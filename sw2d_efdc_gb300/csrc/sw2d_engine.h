@@ -128,6 +128,8 @@ class Engine32 {
     double last_ms_ = 0.0;
     long long last_iters_ = 0;
     int seg_rows_ = 0;
+    void* pin_ = nullptr;      /* pinned staging of state downloads */
+    size_t pin_bytes_ = 0;
     bool tuning_ = false;                       /* a scratch engine of the autotuner */
     std::map<std::pair<int, int>, int> seg_cache_; /* size bucket -> tuned rows per work item */
 };

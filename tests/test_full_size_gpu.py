@@ -76,7 +76,11 @@ def test_fp64_full_raster_wet_regime_properties(pondbreak):
     m.close()
 
 
-def test_fp32_full_raster_balance_and_reproducibility():
+def test_fp32_full_raster_balance_and_reproducibility(monkeypatch):
+    # the rows per work item fixed: the autotuner's timed choice may differ
+    # between two engines, and the tile datum (hence binary32 rounding of the
+    # bed) follows the work items
+    monkeypatch.setenv("SW2D_SEGMENT_ROWS", "256")
     sc = synth.config3(8192, 8192)
     ms = [_model(sc, api.FP32) for _ in range(2)]
     for m in ms:
