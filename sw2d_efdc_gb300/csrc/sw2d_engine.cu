@@ -451,11 +451,22 @@ int Engine32::rebuild(std::string* err) {
             if (fp32_feature_class(d) != k) continue;
             d.first_work = (int)work_.size();
             for (int ty = 0; ty < d.tiles_y; ty++)
-                for (int tx = 0; tx < d.tiles_x; tx++) work_.push_back(make_int4((int)i, tx, ty, 0));
+                for (int tx = 0; tx < d.tiles_x; tx++)
+                    work_.push_back(make_int4((int)i, tx, ty, (int)work_.size() - class_first_[k]));
             d.nwork = (int)work_.size() - d.first_work;
             host[i] = d;
         }
         class_n_[k] = (int)work_.size() - class_first_[k];
+        /* launch the class's longest work items first (a scenario's last
+         * segment is shorter), so that the last wave of CTAs is not left
+         * with long items; .w keeps each item's slot in the scenario-ordered
+         * partials that k32_finalize reduces */
+        auto rows_of = [&](const int4& w) {
+            const Scn32& d = scn_[w.x]->d;
+            return std::min(d.seg, d.R - w.z * d.seg);
+        };
+        std::stable_sort(work_.begin() + class_first_[k], work_.end(),
+                         [&](const int4& a, const int4& b) { return rows_of(a) > rows_of(b); });
     }
     if (host.size() > d_scn_cap_) {
         cudaFree(d_scn_);

@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
     if (!sl.active) {
         if (tid == 0) {
             Part32 zp = {};
-            part[blockIdx.x] = zp;
+            part[w.w] = zp;
         }
         return;
     }
@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         }
         pr.sx = mx * rdxy.x; /* rdx > 0: the maximum commutes with the scaling */
         pr.sy = my * rdxy.y;
-        part[blockIdx.x] = pr;
+        part[w.w] = pr; /* the partials stay in scenario order whatever the launch order */
     }
 }
 
