@@ -168,6 +168,7 @@ int sw2d_batch_create(int device, double hbm_budget_bytes, int max_running, sw2d
     b->budget = hbm_budget_bytes;
     b->max_running = max_running;
     b->eng.reset(new sw2d::Engine32(device));
+    b->eng->set_small_segment_rows(256); /* many scenarios: fewer halo rows beat more work items */
     std::string err;
     int rc = b->eng->init(&err);
     if (rc) return bfail(rc, err);

@@ -101,6 +101,9 @@ class Engine32 {
     /* rows per work item of scenarios added from now on (0 = chosen by
      * segment_rows_for) */
     void set_segment_rows(int rows) { seg_rows_ = rows; }
+    /* rows per work item of rasters below 1 Mcell (128 by default: a lone
+     * small raster needs the parallelism; a batch of many has it anyway) */
+    void set_small_segment_rows(int rows) { small_seg_ = rows; }
     /* Rows per work item for a raster of this size: the fixed value when one
      * is set, else the autotuned choice (timed once per power-of-two size
      * bucket on a scratch scenario) for rasters of >= 1 Mcell, else 128. */
@@ -128,6 +131,7 @@ class Engine32 {
     double last_ms_ = 0.0;
     long long last_iters_ = 0;
     int seg_rows_ = 0;
+    int small_seg_ = 128;
     void* pin_ = nullptr;      /* pinned staging of state downloads */
     size_t pin_bytes_ = 0;
     bool tuning_ = false;                       /* a scratch engine of the autotuner */
