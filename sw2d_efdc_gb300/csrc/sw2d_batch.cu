@@ -21,6 +21,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -169,6 +170,7 @@ int sw2d_batch_create(int device, double hbm_budget_bytes, int max_running, sw2d
     b->max_running = max_running;
     b->eng.reset(new sw2d::Engine32(device));
     b->eng->set_small_segment_rows(256); /* many scenarios: fewer halo rows beat more work items */
+    if (!std::getenv("SW2D_SEGMENT_ROWS")) b->eng->set_segment_rows(256);
     std::string err;
     int rc = b->eng->init(&err);
     if (rc) return bfail(rc, err);
