@@ -353,6 +353,7 @@ def run_batched_leg(args, peak, fp64_value):
     specs = make_batch_specs(args.batch_n, 128, 2048, 4)
     gen_s = time.time() - t0
     b = api.Batch(device=device())
+    b.set_rows_per_item(256)  # the scenarios arrive together: fewer halo rows beat more work items
     for sp in specs:
         b.submit(**sp)
     b.step(0)
@@ -366,11 +367,12 @@ def run_batched_leg(args, peak, fp64_value):
     cu = st1["cell_updates"] - st0["cell_updates"]
     b.close()
     value = cu / (ms * 1e-3) / 1e9
-    achieved = value * BYTES_PER_CELL_FP32_CFG3 * 1e9 / 1e9
+    achieved = value * (BYTES_PER_CELL_FP32_CFG3 + 1)  # + the class byte
     return {"value": round(value, 4), "unit": UNIT, "scenarios": len(specs), "cells": int(cells),
             "steps": args.steps, "ms_per_step": round(ms / args.steps, 4),
             "workload": "batched FP32: %d scenarios, side log-uniform 128-2048, fractal DEM, 3-class Voronoi n, "
-                        "gamma hyetographs, per-scenario CFL length, one fused launch per iteration" % len(specs),
+                        "gamma hyetographs, per-scenario CFL length, one fused launch per iteration, "
+                        "256 rows per work item" % len(specs),
             "roofline": {"bound": "hbm", "kernel": "k32_march + k32_finalize", "achieved": round(achieved, 2),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3 + 1},

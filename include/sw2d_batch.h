@@ -72,6 +72,13 @@ int sw2d_batch_poll(sw2d_batch* b, int64_t id, int* status, sw2d_ledger* ledger)
  * qy rows*(cols+1), reference orientation; any pointer may be NULL. */
 int sw2d_batch_result(sw2d_batch* b, int64_t id, double* depth, double* qx, double* qy);
 int sw2d_batch_release(sw2d_batch* b, int64_t id);
+/* Rows per work item of the scenarios admitted from now on; 0 (the default)
+ * chooses per raster: 128 below 1 Mcell, the autotuned value above.  A batch
+ * whose scenarios arrive together runs faster with 256 (fewer halo rows; the
+ * number of scenarios supplies the parallelism); a serving loop with few
+ * scenarios at a time needs the default's shorter items.  The choice fixes
+ * each scenario's tiling, so its results do not depend on the others. */
+int sw2d_batch_set_rows_per_item(sw2d_batch* b, int rows);
 int sw2d_batch_get_stats(sw2d_batch* b, sw2d_batch_stats* out);
 const char* sw2d_batch_last_error(void);
 

@@ -124,6 +124,7 @@ SIGNATURES = {
     "sw2d_batch_poll": (C.c_int, [C.c_void_p, C.c_int64, _ip, C.POINTER(Ledger)]),
     "sw2d_batch_result": (C.c_int, [C.c_void_p, C.c_int64, _dp, _dp, _dp]),
     "sw2d_batch_release": (C.c_int, [C.c_void_p, C.c_int64]),
+    "sw2d_batch_set_rows_per_item": (C.c_int, [C.c_void_p, C.c_int]),
     "sw2d_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
     "sw2d_batch_last_error": (C.c_char_p, []),
     "sw2d_write_efdc_concentration": (C.c_int, [C.c_char_p, C.c_char, C.c_int, C.c_int, C.c_double, C.c_int, _ip,
@@ -445,6 +446,10 @@ class Batch:
 
     def release(self, rid):
         _bcheck(load().sw2d_batch_release(self._h, int(rid)), "sw2d_batch_release")
+
+    def set_rows_per_item(self, rows):
+        """Rows per work item of scenarios admitted from now on (0 = default)."""
+        _bcheck(load().sw2d_batch_set_rows_per_item(self._h, int(rows)), "sw2d_batch_set_rows_per_item")
 
     def stats(self) -> dict:
         st = BatchStats()

@@ -169,8 +169,6 @@ int sw2d_batch_create(int device, double hbm_budget_bytes, int max_running, sw2d
     b->budget = hbm_budget_bytes;
     b->max_running = max_running;
     b->eng.reset(new sw2d::Engine32(device));
-    b->eng->set_small_segment_rows(256); /* many scenarios: fewer halo rows beat more work items */
-    if (!std::getenv("SW2D_SEGMENT_ROWS")) b->eng->set_segment_rows(256);
     std::string err;
     int rc = b->eng->init(&err);
     if (rc) return bfail(rc, err);
@@ -328,6 +326,14 @@ int sw2d_batch_release(sw2d_batch* b, int64_t id) {
             break;
         }
     b->reqs.erase(it);
+    return SW2D_OK;
+}
+
+int sw2d_batch_set_rows_per_item(sw2d_batch* b, int rows) {
+    if (!b) return bfail(SW2D_ERR_INVALID, "null batch");
+    if (rows != 0 && (rows < 16 || rows > 4096 || rows % 4 != 0))
+        return bfail(SW2D_ERR_INVALID, "rows per work item: 0, or a multiple of 4 in 16..4096");
+    b->eng->set_segment_rows(rows);
     return SW2D_OK;
 }
 

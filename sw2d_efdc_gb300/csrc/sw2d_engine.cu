@@ -108,7 +108,7 @@ size_t Engine32::scenario_bytes(int rows, int cols, bool rain_field, int outlet_
 int Engine32::segment_rows_for(int rows, int cols) {
     if (seg_rows_ > 0) return seg_rows_;
     if (tuning_) return 128;
-    if ((long long)rows * cols < (1ll << 20)) return small_seg_;
+    if ((long long)rows * cols <= small_cells_) return small_seg_;
     auto bucket = [](int n) {
         int b = 0;
         while ((1 << b) < n) b++;

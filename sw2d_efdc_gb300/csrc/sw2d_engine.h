@@ -101,9 +101,13 @@ class Engine32 {
     /* rows per work item of scenarios added from now on (0 = chosen by
      * segment_rows_for) */
     void set_segment_rows(int rows) { seg_rows_ = rows; }
-    /* rows per work item of rasters below 1 Mcell (128 by default: a lone
-     * small raster needs the parallelism; a batch of many has it anyway) */
-    void set_small_segment_rows(int rows) { small_seg_ = rows; }
+    /* rows per work item of rasters of at most `cells` cells (by default 128
+     * below 1 Mcell: a lone small raster needs the parallelism, a batch of
+     * many has it anyway); larger rasters use the autotuned choice */
+    void set_small_segment_rows(int rows, long long cells) {
+        small_seg_ = rows;
+        small_cells_ = cells;
+    }
     /* Rows per work item for a raster of this size: the fixed value when one
      * is set, else the autotuned choice (timed once per power-of-two size
      * bucket on a scratch scenario) for rasters of >= 1 Mcell, else 128. */
@@ -132,6 +136,7 @@ class Engine32 {
     long long last_iters_ = 0;
     int seg_rows_ = 0;
     int small_seg_ = 128;
+    long long small_cells_ = (1ll << 20) - 1;
     void* pin_ = nullptr;      /* pinned staging of state downloads */
     size_t pin_bytes_ = 0;
     bool tuning_ = false;                       /* a scratch engine of the autotuner */

@@ -116,3 +116,30 @@ def test_cancel_mid_run_frees_the_slot_and_leaves_the_others_unchanged():
         assert np.array_equal(h0, h1) and np.array_equal(qx0, qx1) and np.array_equal(qy0, qy1)
         assert led["time"] == l0["time"] == 60.0
     bt.close()
+
+
+def test_rows_per_item_setting():
+    """A batch of scenarios that arrive together may use longer work items;
+    results then stay the same alone and in the mix, and differ from the
+    default tiling by binary32 rounding of the bed only."""
+    a = scenario(300, 31, 60.0)
+
+    def run(specs, rows):
+        b = api.Batch()
+        b.set_rows_per_item(rows)
+        ids = [b.submit(**s) for s in specs]
+        while b.step(32) != (0, 0):
+            pass
+        out = b.result(ids[-1])[0]
+        b.close()
+        return out
+
+    alone = run([a], 256)
+    mixed = run([scenario(500, 32, 30.0), scenario(140, 33, 90.0), a], 256)
+    assert np.array_equal(alone, mixed)
+    default = run([a], 0)
+    assert np.abs(alone - default).max() < 1e-5
+    b = api.Batch()
+    with pytest.raises(api.Sw2dError):
+        b.set_rows_per_item(30)
+    b.close()
