@@ -121,7 +121,7 @@ def test_cancel_mid_run_frees_the_slot_and_leaves_the_others_unchanged():
 def test_rows_per_item_setting():
     """A batch of scenarios that arrive together may use longer work items;
     results then stay the same alone and in the mix, and differ from the
-    default tiling by binary32 rounding of the bed only."""
+    default tiling (other tile datums) within the FP32 form's 1 mm."""
     a = scenario(300, 31, 60.0)
 
     def run(specs, rows):
@@ -138,7 +138,7 @@ def test_rows_per_item_setting():
     mixed = run([scenario(500, 32, 30.0), scenario(140, 33, 90.0), a], 256)
     assert np.array_equal(alone, mixed)
     default = run([a], 0)
-    assert np.abs(alone - default).max() < 1e-5
+    assert np.abs(alone - default).max() < 1e-3  # the FP32 form's depth tolerance
     b = api.Batch()
     with pytest.raises(api.Sw2dError):
         b.set_rows_per_item(30)
