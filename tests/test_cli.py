@@ -151,3 +151,44 @@ def test_check_reads_the_reference_example_setup(tmp_path):
     assert got["dt"] == 0.04 and got["timmax"] == 7200.0 and got["efdc"] == 1
     assert got["nrain"] == 176 and got["evaporation"] == 1 and got["nlayers"] >= 1
     assert len(got["sources"]) == 1 and len(got["outlets"]) == 3
+
+
+def test_rain_file_line_rule(tmp_path):
+    """rain.dat: the reference reads (number of line ends - 1) rows after the
+    two header lines, so a file that ends with a line end gets one more row
+    than it holds (here read as zero, where the reference reads uninitialised
+    memory); the default end time follows the same count."""
+    c = small_case(end=(0, 0, 0, 0), rain=np.array([4.0, 2.0, 0.5]), dtrain=10.0)
+    D.write_db(tmp_path, [c])
+    p = tmp_path / "db" / c.name / "SW2D" / "input" / "rain.dat"
+    got = json.loads(run(tmp_path, "--check").stdout)
+    assert got["nrain"] == 3 and got["timmax"] == 20.0
+    p.write_text(p.read_text() + "\n")
+    got = json.loads(run(tmp_path, "--check").stdout)
+    assert got["nrain"] == 4 and got["timmax"] == 30.0 and got["rain_total"] == 6.5
+
+
+def test_setup_values_may_share_a_line_with_their_labels(tmp_path):
+    """setup.dat is read by position: labels are the '#'-delimited blocks and
+    any white space (CR, tabs, blank lines) separates values."""
+    c = small_case()
+    D.write_db(tmp_path, [c])
+    p = tmp_path / "db" / c.name / "setup.dat"
+    text = p.read_text().replace("#\n", "#\t  ").replace("\n", "\r\n\r\n")
+    p.write_text(text)
+    got = json.loads(run(tmp_path, "--check").stdout)
+    events, _, K = D.schedule(c)
+    assert got["iterations"] == K and got["outputs"] == [[k, lab] for k, _, lab in events]
+    assert got["manning"] == c.manning
+
+
+def test_integer_switch_with_a_fraction_is_refused(tmp_path):
+    c = small_case()
+    D.write_db(tmp_path, [c])
+    p = tmp_path / "db" / c.name / "setup.dat"
+    lines = p.read_text().splitlines()
+    k = lines.index("# EVAPORATION SWITCH #") + 1
+    lines[k] = "1.5"
+    p.write_text("\n".join(lines) + "\n")
+    r = run(tmp_path, "--check")
+    assert r.returncode == 1 and "expected an integer" in r.stdout
