@@ -217,9 +217,10 @@ def cpu_reference_sample(sc, iters: int, warm: int, threads: int, h0=None, gpu: 
 
 def reference_gpu_spinup(sc, seconds: float):
     """Depth after `seconds` of simulated time with the reference's own GPU
-    kernels (FIXED dt), or None when that build is unavailable."""
+    kernels (FIXED dt), or None when that build or a GPU is unavailable."""
+    import torch
     from oracle import oracle as O
-    if O.ref_gpu_lib() is None:
+    if O.ref_gpu_lib() is None or not torch.cuda.is_available():
         return None
     res = O.run_reference(_reference_case(sc, None, seconds - 0.01), want_fields=False, gpu=True)
     return res["h"]
@@ -619,9 +620,10 @@ def run_reference(args):
         "config": {"workload": "plain SW2D FP64 4096x4096 dx=2m pond-break", "cells": sc.rows * sc.cols},
         "impl": "reference",
         "cpu_baseline": {"value": round(v, 5), "unit": UNIT, "cores": threads, "kind": "reference",
-                         "sample": "%d iterations of the full raster, reference kernels on the CPU (OpenMP), "
-                                   "from the depth after %.0f s of the reference's own GPU run"
-                                   % (n, args.spinup_s if h_spun is not None else 0.0)},
+                         "sample": "%d iterations of the full raster, reference kernels on the CPU (OpenMP), %s"
+                                   % (n, "from the depth after %.0f s of the reference's own GPU run" % args.spinup_s
+                                      if h_spun is not None else "from the scenario's initial depth (no GPU "
+                                                                 "for the wet spin-up)")},
         "e2e": {"value": round(v, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "reference_gpu": ref_gpu,
     }
