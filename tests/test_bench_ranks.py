@@ -52,3 +52,26 @@ def test_one_rank_needs_no_process_group(monkeypatch):
         monkeypatch.delenv(k, raising=False)
     import bench
     assert bench.device() == 0 and bench.rank_max(3.25) == 3.25
+
+
+def test_reference_arm_line_on_the_cpu():
+    # the reference arm times the reference's own kernels built for the CPU,
+    # here from the scenario's initial depth (no wet spin-up)
+    import json
+    import subprocess
+    import sys
+    from oracle import oracle as O
+    if O.ref_lib() is None:
+        pytest.skip("reference CPU build unavailable")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE")}
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--size", "256", "--steps", "3",
+                          "--warmup", "3", "--spinup-s", "0"], cwd=root, env=env, capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["kind"] == "reference" and line["cpu_baseline"]["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert line["config"]["cells"] == 256 * 256
