@@ -443,7 +443,6 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
     sc = workload_config2(args.size)
     cells = sc.rows * sc.cols
     K = args.steps + (args.steps & 1)
