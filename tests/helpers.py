@@ -49,3 +49,23 @@ def bumpy_case(R=48, C=40, seed=3, holes=True, **kw) -> O.Case:
                 rain=np.array([3.0, 3.0, 3.0, 3.0]), dtrain=3600.0)
     args.update(kw)
     return O.Case(**args)
+
+
+RAGGED_SHAPES = [(3, 5), (4, 2), (21, 37), (64, 17), (2, 33)]
+
+
+def ragged_case(R, C, **kw) -> O.Case:
+    """A few rows or an odd column count (cols/2 padding cells after the
+    raster in the reference's arrays), NODATA on the raster's edges, a cell
+    that starts just at th."""
+    rng = np.random.default_rng(R * 100 + C)
+    dem = 0.02 * (R - np.arange(R))[:, None] + 0.05 * rng.standard_normal((R, C))
+    dem[0, C - 1] = -9999.0
+    dem[R - 1, 0] = -9999.0
+    h0 = np.where(rng.random((R, C)) < 0.3, 0.2 * rng.random((R, C)), 0.0)
+    h0[R // 2, C // 2] = 1e-4
+    h0[dem == -9999.0] = 0.0
+    args = dict(dem=dem, h0=h0, cellsize=5.0, manning=0.04, dt=0.05, t_end=8.0,
+                rain=np.array([12.0, 12.0, 12.0]), dtrain=3.1)
+    args.update(kw)
+    return O.Case(**args)

@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.helpers import bumpy_case
+from tests.helpers import RAGGED_SHAPES, bumpy_case, ragged_case
 
 ref_missing = O.ref_lib() is None
 pytestmark = pytest.mark.skipif(ref_missing, reason="reference CPU build unavailable")
@@ -36,20 +36,9 @@ def test_pin_nonzero_initial_depth_on_nodata_cells():
     _pin(case)
 
 
-@pytest.mark.parametrize("R,C", [(3, 5), (4, 2), (21, 37), (64, 17), (2, 33)])
+@pytest.mark.parametrize("R,C", RAGGED_SHAPES)
 def test_pin_ragged_shapes(R, C):
-    # odd column counts (cols/2 padding cells after the raster), a handful of
-    # rows, NODATA on the raster's edges and a cell that starts just at th
-    rng = np.random.default_rng(R * 100 + C)
-    dem = 0.02 * (R - np.arange(R))[:, None] + 0.05 * rng.standard_normal((R, C))
-    dem[0, C - 1] = -9999.0
-    dem[R - 1, 0] = -9999.0
-    h0 = np.where(rng.random((R, C)) < 0.3, 0.2 * rng.random((R, C)), 0.0)
-    h0[R // 2, C // 2] = 1e-4
-    h0[dem == -9999.0] = 0.0
-    case = O.Case(dem=dem, h0=h0, cellsize=5.0, manning=0.04, dt=0.05, t_end=8.0,
-                  rain=np.array([12.0, 12.0, 12.0]), dtrain=3.1)
-    _pin(case)
+    _pin(ragged_case(R, C))
 
 
 def test_pin_runoff_fractions_and_ramp():
