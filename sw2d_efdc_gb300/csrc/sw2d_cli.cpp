@@ -44,6 +44,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <iostream>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -255,7 +256,9 @@ void read_grid_header(Reader& r, Grid* g) {
     r.keyword("NODATA_value");
     g->nodata = r.need_number("NODATA_value");
     if (g->cols < 1 || g->rows < 1) input_error(r.name() + ": ncols and nrows must be >= 1");
-    if (!(g->cellsize > 0)) input_error(r.name() + ": cellsize must be > 0");
+    /* the library's limit: rows * cols <= 2^30 cells */
+    if ((long long)g->cols * g->rows > (1LL << 30)) input_error(r.name() + ": more than 2^30 cells");
+    if (!(g->cellsize > 0) || !std::isfinite(g->cellsize)) input_error(r.name() + ": cellsize must be > 0");
 }
 
 void read_setup(Case& c) {
@@ -289,8 +292,20 @@ void read_setup(Case& c) {
     if (c.efdc == 1)
         for (int k = 0; k < kNSection2; k++)
             c.s2[k] = kSection2[k].integer ? (double)integ(kSection2[k].name) : num(kSection2[k].name);
-    if (!(c.dt > 0)) input_error("setup.dat: TIME STEP must be > 0");
+    if (!(c.dt > 0) || !std::isfinite(c.dt)) input_error("setup.dat: TIME STEP must be > 0");
 }
+
+/* round(interval / dt) as the reference's integer step counts; an interval
+ * that is not a positive number of steps gives 0, one beyond 2^62 steps
+ * gives 2^62 (never reached) */
+long steps_of(double interval, double dt) {
+    const double v = std::round(interval / dt);
+    if (!(v >= 1.0)) return 0;
+    return v > 4.6e18 ? (1L << 62) : (long)v;
+}
+
+constexpr double kMaxIterations = 1e10;
+constexpr double kMaxRecords = 1e8;
 
 /* the reference's point-source and outlet cell rule (stream_flow,
  * SW2D-EFDC.cu:540-544; outlets :4990-4993): column round(|x0 - x|),
@@ -426,9 +441,19 @@ void read_inputs(Case& c) {
     c.time0 = 3600.0 * 24.0 * c.t0[0] + 3600.0 * c.t0[1] + 60.0 * c.t0[2] + c.t0[3];
     c.timmax = 3600.0 * 24.0 * c.t1[0] + 3600.0 * c.t1[1] + 60.0 * c.t1[2] + c.t1[3];
     if (c.t1[0] == 0 && c.t1[1] == 0 && c.t1[2] == 0 && c.t1[3] == 0) c.timmax = (double)(nrain - 1) * c.dtrain;
-    c.lpout = (long)std::round(c.dpout / c.dt);
-    c.lkout = (long)std::round(c.dkout / c.dt);
+    c.lpout = steps_of(c.dpout, c.dt);
+    c.lkout = steps_of(c.dkout, c.dt);
     if (c.lkout < 1) input_error("setup.dat: TIME INTERVAL TO WRITE THE RESULTS must be at least half a TIME STEP");
+    if (!c.src_cells.empty() && !(c.dtoq > 0 && std::isfinite(c.dtoq)))
+        input_error("setup.dat: TEMPORAL RESOLUTION OF FLOW INPUT DATA must be > 0 with point sources");
+    if (!std::isfinite(c.time0) || !std::isfinite(c.timmax)) input_error("setup.dat: the start and end times must be finite");
+    /* the schedule is walked iteration by iteration (the reference's time
+     * accumulation); bound the walk and what it keeps */
+    const double iters = (c.timmax - c.time0) / (2.0 * c.dt);
+    if (iters > kMaxIterations) input_error("setup.dat: the run needs more than 1e10 iterations");
+    if (iters > 0 && (2.0 * iters / (double)c.lkout > kMaxRecords ||
+                      (c.lpout > 0 && 2.0 * iters / (double)c.lpout > kMaxRecords)))
+        input_error("setup.dat: more than 1e8 result or progress records");
 }
 
 /* ------------------------------------------------------------ schedule */
@@ -831,6 +856,10 @@ int main(int argc, char** argv) {
     } catch (const LibError& e) {
         std::fflush(stdout);
         std::fprintf(stderr, "sw2d_cli: %s\n", e.msg.c_str());
+        return 2;
+    } catch (const std::bad_alloc&) {
+        std::fflush(stdout);
+        std::fprintf(stderr, "sw2d_cli: out of host memory\n");
         return 2;
     }
     return 0;
