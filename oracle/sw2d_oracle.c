@@ -73,17 +73,14 @@ static double series_at(const double* v, int n, double dts, double time, int mod
         if (time <= 1.00) {
             r = v[0] * time;
         } else {
-            it = (int)(time / dts);
-            if (it + 1 > n) it = n; /* past the series: zero tail */
+            it = sw2d_series_index(time, dts, n); /* past the series: zero tail */
             r = v[it] + (v[it + 1] - v[it]) / (dts * (time - dts * (it)));
         }
     } else if (mode == ORC_RAIN_LINEAR) {
-        it = (int)(time / dts);
-        if (it + 1 > n) it = n;
+        it = sw2d_series_index(time, dts, n);
         r = v[it] + (v[it + 1] - v[it]) * ((time - dts * (it)) / dts);
     } else {
-        it = (int)(time / dts);
-        if (it > n) it = n;
+        it = sw2d_series_index(time, dts, n);
         r = v[it];
     }
     return r;
@@ -107,15 +104,13 @@ static void source_rates(const orc_state* s, double time, double* ql) {
             if (time <= 1.00) {
                 q = s->srcq[i] * time;
             } else {
-                int it = (int)(time / s->c.dtoq);
-                if (it + 1 > s->c.nq) it = s->c.nq;
+                const int it = sw2d_series_index(time, s->c.dtoq, s->c.nq);
                 q = s->srcq[(size_t)it * s->c.nsrc + i] +
                     (s->srcq[(size_t)(it + 1) * s->c.nsrc + i] - s->srcq[(size_t)it * s->c.nsrc + i]) /
                         (s->c.dtoq * (time - s->c.dtoq * (it)));
             }
         } else {
-            int it = (int)(time / s->c.dtoq);
-            if (it + 1 > s->c.nq) it = s->c.nq;
+            const int it = sw2d_series_index(time, s->c.dtoq, s->c.nq);
             double a = s->srcq[(size_t)it * s->c.nsrc + i];
             if (s->c.rain_mode == ORC_RAIN_LINEAR) {
                 double b = s->srcq[(size_t)(it + 1) * s->c.nsrc + i];

@@ -27,6 +27,7 @@
  * the tile datum, so no large elevations are added to small depths.
  */
 #include "sw2d_fp32.h"
+#include "sw2d_math.h"
 
 #include <math.h>
 #include <stddef.h>
@@ -664,16 +665,13 @@ __device__ double series_at32(const double* v, int n, double dts, double time, i
     int it;
     if (mode == 0) {
         if (time <= 1.00) return v[0] * time;
-        it = (int)(time / dts);
-        if (it + 1 > n) it = n;
+        it = sw2d_series_index(time, dts, n);
         return v[it] + (v[it + 1] - v[it]) / (dts * (time - dts * (it)));
     } else if (mode == 1) {
-        it = (int)(time / dts);
-        if (it + 1 > n) it = n;
+        it = sw2d_series_index(time, dts, n);
         return v[it] + (v[it + 1] - v[it]) * ((time - dts * (it)) / dts);
     }
-    it = (int)(time / dts);
-    if (it > n) it = n;
+    it = sw2d_series_index(time, dts, n);
     return v[it];
 }
 
@@ -686,8 +684,7 @@ __device__ float source_at32(const Scn32& P, int i, double time) {
     if (P.series_mode == 0 && time <= 1.00) {
         q = Q[i] * time;
     } else {
-        int it = (int)(time / P.dtoq);
-        if (it + 1 > P.nq) it = P.nq;
+        const int it = sw2d_series_index(time, P.dtoq, P.nq);
         const double a = Q[(size_t)it * ns + i], b = Q[(size_t)(it + 1) * ns + i];
         if (P.series_mode == 0)
             q = a + (b - a) / (P.dtoq * (time - P.dtoq * (it)));

@@ -35,17 +35,14 @@ __device__ __forceinline__ double series_at(const double* v, int n, double dts, 
         if (time <= 1.00) {
             r = v[0] * time;
         } else {
-            it = (int)(time / dts);
-            if (it + 1 > n) it = n;
+            it = sw2d_series_index(time, dts, n);
             r = v[it] + (v[it + 1] - v[it]) / (dts * (time - dts * (it)));
         }
     } else if (mode == 1) {
-        it = (int)(time / dts);
-        if (it + 1 > n) it = n;
+        it = sw2d_series_index(time, dts, n);
         r = v[it] + (v[it + 1] - v[it]) * ((time - dts * (it)) / dts);
     } else {
-        it = (int)(time / dts);
-        if (it > n) it = n;
+        it = sw2d_series_index(time, dts, n);
         r = v[it];
     }
     return r;
@@ -59,14 +56,12 @@ __device__ __forceinline__ double source_at(const StepParams& p, int i, double t
         if (time <= 1.00) {
             q = Q[i] * time;
         } else {
-            int it = (int)(time / p.dtoq);
-            if (it + 1 > p.nq) it = p.nq;
+            const int it = sw2d_series_index(time, p.dtoq, p.nq);
             q = Q[(size_t)it * ns + i] + (Q[(size_t)(it + 1) * ns + i] - Q[(size_t)it * ns + i]) /
                                              (p.dtoq * (time - p.dtoq * (it)));
         }
     } else {
-        int it = (int)(time / p.dtoq);
-        if (it + 1 > p.nq) it = p.nq;
+        const int it = sw2d_series_index(time, p.dtoq, p.nq);
         double a = Q[(size_t)it * ns + i];
         if (p.series_mode == 1) {
             double b = Q[(size_t)(it + 1) * ns + i];

@@ -37,6 +37,17 @@
 #define SW2D_HD static inline
 #endif
 
+/* Index of the series entry in force at `time` (one entry every dts
+ * seconds), clamped to n, the first entry of the series' zero tail: the
+ * reference's int(time / dts) (SW2D-EFDC.cu:537, :550) without reading past
+ * the series.  The clamp is decided in binary64, so a quotient beyond the
+ * int range (a long run with a short series interval) clamps instead of
+ * converting out of range. */
+SW2D_HD int sw2d_series_index(double time, double dts, int n) {
+    const double f = time / dts;
+    return f >= (double)n ? n : (int)f;
+}
+
 /* 1.3333330 - 4/3 evaluated exactly (binary64 value of 1.3333330 minus the
  * real 4/3), then rounded to binary64. */
 #define SW2D_POW_RESIDUAL (-3.3333333323189623e-07)

@@ -132,3 +132,22 @@ def test_threshold_comparisons_match_ieee(mathlib):
         L.cmpp(a.ctypes.data_as(dp), t, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), a.size)
         ref = (a > t).astype(int) | (a < t) << 1 | (a >= t) << 2 | (a <= t) << 3
         assert np.array_equal(out, ref), t
+
+
+def test_series_index_clamps_beyond_the_int_range():
+    # a 1 ns source interval 5 s into the run: time / dtoq is 5e9, past the
+    # int range; the lookup clamps to the zero tail, so the sources add
+    # nothing and the run equals the run without them
+    from oracle import oracle as O
+    from tests.helpers import bumpy_case
+    for mode in (O.RAIN_REFERENCE, O.RAIN_LINEAR, O.RAIN_STEP):
+        base = dict(R=24, C=20, seed=31, holes=False, t0=5.0, t_end=9.0, dt=0.05, rain_mode=mode)
+        with_src = bumpy_case(**base)
+        with_src.src_cell = np.array([5 * 20 + 7, 12 * 20 + 3], np.int32)
+        with_src.src_q = np.array([[0.5, 0.2], [0.8, 0.4], [0.3, 0.1]])
+        with_src.dtoq = 1e-9
+        plain = bumpy_case(**base)
+        a, b = O.Oracle(with_src), O.Oracle(plain)
+        assert a.run() == b.run() > 0
+        assert np.array_equal(a.fields()["h"], b.fields()["h"])
+        assert a.ledger()["source_in"] == 0.0
