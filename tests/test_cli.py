@@ -192,3 +192,41 @@ def test_integer_switch_with_a_fraction_is_refused(tmp_path):
     p.write_text("\n".join(lines) + "\n")
     r = run(tmp_path, "--check")
     assert r.returncode == 1 and "expected an integer" in r.stdout
+
+
+@pytest.mark.parametrize("rel,old,new,msg", [
+    ("SW2D/input/dem.dat", "ncols         11", "ncols         100000000", "more than 2^30 cells"),
+    ("SW2D/input/dem.dat", "nrows         14", "nrows         2147483647", "more than 2^30 cells"),
+    ("setup.dat", "# END: DAYS HOURS MINUTES SECONDS #\n0 0 0 20",
+     "# END: DAYS HOURS MINUTES SECONDS #\n0 0 0 1e12", "more than 1e10 iterations"),
+    ("setup.dat", "# END: DAYS HOURS MINUTES SECONDS #\n0 0 0 20",
+     "# END: DAYS HOURS MINUTES SECONDS #\n0 0 0 nan", "must be finite"),
+    ("setup.dat", "# TIME STEP #\n0.05", "# TIME STEP #\n1e-300", "more than 1e10 iterations"),
+    ("setup.dat", "# TIME STEP #\n0.05", "# TIME STEP #\ninf", "TIME STEP must be > 0"),
+    ("setup.dat", "# SOURCE SERIES INTERVAL (S) #\n10.0", "# SOURCE SERIES INTERVAL (S) #\n0",
+     "FLOW INPUT DATA must be > 0"),
+    ("setup.dat", "# END: DAYS HOURS MINUTES SECONDS #\n0 0 0 20\n# TIME STEP #\n0.05\n# PROGRESS INTERVAL (S) #\n2.0\n"
+                  "# RESULTS INTERVAL (S) #\n3.0",
+     "# END: DAYS HOURS MINUTES SECONDS #\n0 0 0 1e7\n# TIME STEP #\n0.05\n# PROGRESS INTERVAL (S) #\n2.0\n"
+     "# RESULTS INTERVAL (S) #\n0.05", "1e8 result"),
+])
+def test_out_of_range_values_stop_with_a_message(tmp_path, rel, old, new, msg):
+    # values the reference would overflow, divide by zero or loop on for ever
+    c = small_case()
+    D.write_db(tmp_path, [c])
+    p = tmp_path / "db" / c.name / rel
+    text = p.read_text()
+    assert old in text
+    p.write_text(text.replace(old, new, 1))
+    r = run(tmp_path, "--check")
+    assert r.returncode == 1 and msg in r.stdout, (r.returncode, r.stdout, r.stderr)
+
+
+def test_a_huge_results_interval_writes_only_the_first_record(tmp_path):
+    c = small_case()
+    D.write_db(tmp_path, [c])
+    p = tmp_path / "db" / c.name / "setup.dat"
+    p.write_text(p.read_text().replace("# RESULTS INTERVAL (S) #\n3.0", "# RESULTS INTERVAL (S) #\n1e300", 1))
+    r = run(tmp_path, "--check")
+    assert r.returncode == 0, r.stdout
+    assert json.loads(r.stdout)["outputs"] == [[1, "0"]]
