@@ -873,7 +873,8 @@ int sw2d_set_rain_series(sw2d_handle* h, const double* mm, int n, double dtrain)
     }
     int rc = set_device(h);
     if (rc) return rc;
-    std::vector<double> v(n + 2, 0.0);
+    /* nrain entries and the two-entry zero tail the clamped lookup reads */
+    std::vector<double> v((size_t)std::max(n, 1) + 2, 0.0);
     for (int k = 0; k < n; k++) v[k] = mm[k];
     dfree(h->rain);
     if ((rc = dalloc(&h->rain, v.size()))) return rc;
