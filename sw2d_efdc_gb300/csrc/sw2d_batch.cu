@@ -185,6 +185,10 @@ int sw2d_batch_submit(sw2d_batch* b, const sw2d_scenario* s, int64_t* id_out) {
     if (!b || !s || !s->dem) return bfail(SW2D_ERR_INVALID, "null argument");
     if (s->rows < 2 || s->cols < 2 || !(s->dx > 0) || !(s->dy > 0) || !(s->th > 0))
         return bfail(SW2D_ERR_INVALID, "scenario geometry");
+    if ((long long)s->rows * s->cols > (1LL << 30)) return bfail(SW2D_ERR_INVALID, "raster too large");
+    if (s->dt_mode != SW2D_DT_FIXED && s->dt_mode != SW2D_DT_CFL) return bfail(SW2D_ERR_INVALID, "dt_mode");
+    if (s->series_mode < 0 || s->series_mode > 2) return bfail(SW2D_ERR_INVALID, "series_mode");
+    if (s->outlet_capacity < 0) return bfail(SW2D_ERR_INVALID, "outlet_capacity");
     if (s->manning_class && (!s->manning_table || s->ntable <= 0 || s->ntable > 64))
         return bfail(SW2D_ERR_INVALID, "Manning table must have 1..64 entries");
     if ((s->nrain > 0 && !s->rain_mm) || s->nrain < 0 || !(s->dtrain > 0))
