@@ -230,3 +230,29 @@ def test_a_huge_results_interval_writes_only_the_first_record(tmp_path):
     r = run(tmp_path, "--check")
     assert r.returncode == 0, r.stdout
     assert json.loads(r.stdout)["outputs"] == [[1, "0"]]
+
+
+def test_truncated_or_corrupted_inputs_end_with_a_status_never_a_signal(tmp_path):
+    # every input file of a coupled case with evaporation, cut short or given
+    # a stray token at a seeded position: status 0 or 1 (with a message)
+    import random
+    rng = random.Random(7)
+    c = small_case(efdc=1, evaporation_on=1, temp=np.array([20.0, 22.0, 25.0, 21.0]),
+                   rad=np.array([100.0, 500.0, 700.0, 0.0]), mask=np.pad(np.ones((4, 4), np.int32), ((5, 5), (3, 4))),
+                   template=b"C22 X\n1\nC23 Y\n2\nC24 Z\n3\nC25 W\n4\nC26 V\n5\nC27 U\n6\n",
+                   section2={"efdc_basetime": 3600.0, "nlayers": 3, "dye_on": 1, "temp_on": 1, "salt_on": 1})
+    D.write_db(tmp_path, [c])
+    files = sorted(p for p in (tmp_path / "db").rglob("*") if p.is_file())
+    originals = {p: p.read_bytes() for p in files}
+    assert run(tmp_path, "--check").returncode == 0
+    for p in files:
+        data = originals[p]
+        for _ in range(6):
+            k = rng.randrange(0, max(1, len(data)))
+            bad = data[:k] if rng.random() < 0.5 else data[:k] + rng.choice(
+                [b" abc ", b"\x00", b" 1e400 ", b" nan ", b" -7 ", b"####", b" 99999999999 ", b"\n"]) + data[k:]
+            p.write_bytes(bad)
+            r = run(tmp_path, "--check")
+            assert r.returncode in (0, 1), (p.name, k, r.returncode, r.stderr[-300:])
+            assert r.returncode == 0 or r.stdout.strip(), (p.name, k)
+        p.write_bytes(data)
