@@ -142,3 +142,23 @@ def test_device_math_flavour_tracks_the_reference_flavour_on_long_runs():
         ol.run()
         assert od.iters > 1000 and abs(od.iters - ol.iters) <= 1
         assert np.abs(od.fields()["h"] - ol.fields()["h"]).max() <= 1e-9
+
+
+@pytest.mark.parametrize("seed", range(40))
+def test_pin_random_cases(seed):
+    # seeded random shapes, NODATA patterns, initial ponds, runoff fractions,
+    # rain series (length, interval) and time steps
+    rng = np.random.default_rng(1000 + seed)
+    R, C = int(rng.integers(2, 41)), int(rng.integers(2, 41))
+    dem = rng.uniform(-0.5, 0.5) * np.arange(R)[:, None] + 0.1 * rng.standard_normal((R, C)).cumsum(1)
+    dem[rng.random((R, C)) < rng.uniform(0, 0.15)] = -9999.0
+    h0 = np.where(rng.random((R, C)) < rng.uniform(0, 0.5), rng.uniform(0, 0.5) * rng.random((R, C)), 0.0)
+    h0[dem == -9999.0] = 0.0
+    nrain = int(rng.integers(1, 8))
+    frac = rng.uniform(0, 0.3, 3) if rng.random() < 0.5 else np.zeros(3)
+    case = O.Case(dem=dem, h0=h0, cellsize=float(rng.choice([1.0, 2.5, 5.0, 10.0])),
+                  manning=float(rng.uniform(0.01, 0.1)), dt=float(rng.choice([0.01, 0.02, 0.05])),
+                  t_end=float(rng.uniform(1.5, 6.0)), rain=rng.uniform(0, 20, nrain),
+                  dtrain=float(rng.uniform(0.7, 5.0)), frac_int=frac[0], frac_inf=frac[1], frac_lwl=frac[2],
+                  ev_wl_min=float(rng.uniform(0.0, 0.1)))
+    _pin(case)
