@@ -156,9 +156,54 @@ def test_pin_random_cases(seed):
     h0[dem == -9999.0] = 0.0
     nrain = int(rng.integers(1, 8))
     frac = rng.uniform(0, 0.3, 3) if rng.random() < 0.5 else np.zeros(3)
+    t_end = float(rng.uniform(1.5, 6.0))
     case = O.Case(dem=dem, h0=h0, cellsize=float(rng.choice([1.0, 2.5, 5.0, 10.0])),
                   manning=float(rng.uniform(0.01, 0.1)), dt=float(rng.choice([0.01, 0.02, 0.05])),
-                  t_end=float(rng.uniform(1.5, 6.0)), rain=rng.uniform(0, 20, nrain),
-                  dtrain=float(rng.uniform(0.7, 5.0)), frac_int=frac[0], frac_inf=frac[1], frac_lwl=frac[2],
-                  ev_wl_min=float(rng.uniform(0.0, 0.1)))
+                  t_end=t_end, rain=rng.uniform(0, 20, nrain), dtrain=_inside(rng, t_end, nrain),
+                  frac_int=frac[0], frac_inf=frac[1], frac_lwl=frac[2], ev_wl_min=float(rng.uniform(0.0, 0.1)))
     _pin(case)
+
+
+def _inside(rng, t_end, n):
+    """A series interval that keeps a run of t_end inside a series of n
+    entries: the reference reads entries it and it + 1 with no bound
+    (SW2D-EFDC.cu:537, :550), so past the series it reads beyond its arrays,
+    where this library reads the series' zero tail."""
+    return float(t_end / n * rng.uniform(1.05, 3.0))
+
+
+@pytest.mark.parametrize("seed", range(20))
+def test_pin_random_cases_with_sources_and_evaporation(seed):
+    rng = np.random.default_rng(2000 + seed)
+    R, C = int(rng.integers(3, 36)), int(rng.integers(3, 36))
+    dem = rng.uniform(-0.3, 0.3) * np.arange(R)[:, None] + 0.08 * rng.standard_normal((R, C)).cumsum(1)
+    dem[rng.random((R, C)) < 0.05] = -9999.0
+    h0 = np.where(rng.random((R, C)) < 0.3, 0.3 * rng.random((R, C)), 0.0)
+    h0[dem == -9999.0] = 0.0
+    nrain = int(rng.integers(2, 7))
+    t_end = float(rng.uniform(2.0, 6.0))
+    dtrain = _inside(rng, t_end, nrain)
+    case = O.Case(dem=dem, h0=h0, cellsize=1.0, manning=float(rng.uniform(0.02, 0.08)), dt=0.02,
+                  t_end=t_end, rain=rng.uniform(0, 10, nrain), dtrain=dtrain,
+                  frac_lwl=float(rng.uniform(0, 0.3)), ev_wl_min=float(rng.uniform(0.0, 0.05)))
+    kw = {}
+    # point sources in the reference's coordinates (x from the west edge, y
+    # from the south edge, in cells): id = qiny*cols + qinx + 1
+    nsrc = int(rng.integers(1, 4))
+    brx = rng.integers(0, C - 1, nsrc).astype(float)
+    bry = rng.integers(1, R, nsrc).astype(float)
+    nq = int(rng.integers(2, 6))
+    qq = rng.uniform(-0.05, 0.4, (nq, nsrc))
+    dtoq = _inside(rng, t_end, nq)
+    case.src_cell = np.array([(R - round(y)) * C + round(x) + 1 for x, y in zip(brx, bry)], np.int32)
+    case.src_q = qq
+    case.dtoq = dtoq
+    kw["sources"] = (brx, bry, qq, dtoq, 0.0, 0.0)
+    if rng.random() < 0.6:
+        T = rng.uniform(10, 30, nrain)
+        Rg = rng.uniform(0, 900, nrain)
+        albedo = float(rng.uniform(0.05, 0.3))
+        from sw2d_efdc_gb300 import api
+        case.evap = api.evaporation_series(T, Rg, albedo, dtrain)
+        kw["evap_inputs"] = (T, Rg, albedo)
+    _pin(case, **kw)
