@@ -228,7 +228,7 @@ struct Case {
     std::vector<long long> outlet_cell; /* raster id each outlet's depth is read at; <0 = outside */
     int n_out = 0;
     std::vector<int> mask;
-    /* times (SW2D-EFDC.cu:4217-4222, :4620-4621) */
+    /* times (SW2D-EFDC.cu:4230-4234) and step counts (:4187-4188) */
     double time0 = 0, timmax = 0;
     long lpout = 0, lkout = 0;
 
@@ -437,7 +437,7 @@ void read_inputs(Case& c) {
         if ((int)c.s2v("nlayers") < 1) input_error("setup.dat: NUMBER OF VERTICAL LAYERS must be >= 1");
         if (!(c.s2v("efdc_basetime") > 0)) input_error("setup.dat: EFDC BASE TIME must be > 0");
     }
-    /* times and output intervals (SW2D-EFDC.cu:4217-4222, :4620-4621) */
+    /* times (SW2D-EFDC.cu:4230-4234) and output intervals in steps (:4187-4188) */
     c.time0 = 3600.0 * 24.0 * c.t0[0] + 3600.0 * c.t0[1] + 60.0 * c.t0[2] + c.t0[3];
     c.timmax = 3600.0 * 24.0 * c.t1[0] + 3600.0 * c.t1[1] + 60.0 * c.t1[2] + c.t1[3];
     if (c.t1[0] == 0 && c.t1[1] == 0 && c.t1[2] == 0 && c.t1[3] == 0) c.timmax = (double)(nrain - 1) * c.dtrain;
