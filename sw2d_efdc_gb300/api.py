@@ -181,6 +181,7 @@ class Model:
 
     def __init__(self, cfg: Config):
         L = load()
+        self._nfaces = 0
         h = C.c_void_p()
         _check(L.sw2d_create(C.byref(cfg), C.byref(h)), "sw2d_create")
         self._h = h
@@ -242,8 +243,12 @@ class Model:
                "sw2d_set_evaporation_series")
 
     def set_point_sources(self, cells, q, dtoq):
-        cells = np.ascontiguousarray(cells, np.int32)
+        """Raster ids (row * cols + col) of the sources and their discharges
+        (m3/s), one row of len(cells) values per interval of dtoq seconds."""
+        cells = np.ascontiguousarray(cells, np.int32).reshape(-1)
         q = np.ascontiguousarray(q, np.float64)
+        if len(cells) and (q.ndim != 2 or q.shape[0] < 1 or q.shape[1] != len(cells)):
+            raise ValueError("q must have shape (intervals, %d), got %s" % (len(cells), q.shape))
         nq = q.shape[0] if len(cells) else 0
         _check(load().sw2d_set_point_sources(self._h, len(cells), _ptr(cells, _ip), _ptr(q, _dp), nq,
                                              float(dtoq)), "sw2d_set_point_sources")
@@ -390,7 +395,16 @@ class Batch:
                nodata=-9999.0, th=1e-4, g=9.80, outlet_capacity=0, frac_int=0.0, frac_inf=0.0,
                frac_lwl=0.0, ev_wl_min=0.05) -> int:
         dem = np.ascontiguousarray(dem, np.float64)
+        if dem.ndim != 2:
+            raise ValueError("dem must be a (rows, cols) array, got shape %s" % (dem.shape,))
         R, Cc = dem.shape
+
+        def grid(a, dtype, what):
+            a = np.ascontiguousarray(a, dtype)
+            if a.shape != (R, Cc):
+                raise ValueError("%s must have the dem's shape %s, got %s" % (what, (R, Cc), a.shape))
+            return a
+
         keep = [dem]
         s = Scenario()
         s.rows, s.cols = R, Cc
@@ -404,19 +418,19 @@ class Batch:
         s.outlet_capacity = outlet_capacity
         s.dem = _ptr(dem, _dp)
         if depth is not None:
-            depth = np.ascontiguousarray(depth, np.float64)
+            depth = grid(depth, np.float64, "depth")
             keep.append(depth)
             s.depth = _ptr(depth, _dp)
         if manning_classes is not None:
-            cl = np.ascontiguousarray(manning_classes, np.uint8)
-            tb = np.ascontiguousarray(manning_table, np.float64)
+            cl = grid(manning_classes, np.uint8, "manning_classes")
+            tb = np.ascontiguousarray(manning_table, np.float64).reshape(-1)
             keep += [cl, tb]
             s.manning_class, s.manning_table, s.ntable = _ptr(cl, _u8p), _ptr(tb, _dp), len(tb)
-        rain = np.ascontiguousarray(rain_mm, np.float64)
+        rain = np.ascontiguousarray(rain_mm, np.float64).reshape(-1)
         keep.append(rain)
         s.rain_mm, s.nrain = _ptr(rain, _dp), len(rain)
         if rain_weight is not None:
-            w = np.ascontiguousarray(rain_weight, np.float32)
+            w = grid(rain_weight, np.float32, "rain_weight")
             keep.append(w)
             s.rain_weight = _ptr(w, _fp)
         rid = C.c_int64(0)

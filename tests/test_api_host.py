@@ -1,0 +1,78 @@
+"""Host-side argument checks of the Python mirror (api.py) on the CPU: the C
+ABI cannot know the length of a host array, so shapes are checked before
+any call reaches the library.  A recording stand-in replaces the library."""
+import numpy as np
+import pytest
+
+from sw2d_efdc_gb300 import api
+
+
+class _Recorder:
+    def __init__(self):
+        self.calls = []
+
+    def __getattr__(self, name):
+        def f(*args):
+            self.calls.append(name)
+            return 0
+        return f
+
+
+@pytest.fixture
+def lib(monkeypatch):
+    rec = _Recorder()
+    monkeypatch.setattr(api, "load", lambda *a: rec)
+    return rec
+
+
+def _model(R=6, C=5):
+    m = object.__new__(api.Model)
+    m._h = api.C.c_void_p(0)
+    m.rows, m.cols, m._nfaces = R, C, 0
+    return m
+
+
+def test_point_sources_need_one_column_per_source(lib):
+    m = _model()
+    m.set_point_sources([3, 7], np.zeros((4, 2)), 60.0)
+    m.set_point_sources([], np.zeros((0,)), 60.0)
+    assert lib.calls == ["sw2d_set_point_sources"] * 2
+    for q in (np.zeros(4), np.zeros((4, 3)), np.zeros((0, 2))):
+        with pytest.raises(ValueError):
+            m.set_point_sources([3, 7], q, 60.0)
+    assert len(lib.calls) == 2
+
+
+def test_grids_must_match_the_raster(lib):
+    m = _model()
+    m.set_dem(np.zeros((6, 5)))
+    for f in (m.set_dem, m.set_depth, m.set_rain_field, m.set_coupling_mask):
+        with pytest.raises(ValueError):
+            f(np.zeros((5, 6)))
+    with pytest.raises(ValueError):
+        m.set_manning_classes(np.zeros((6, 4), np.uint8), [0.03])
+    assert lib.calls == ["sw2d_set_dem"]
+
+
+def test_coupling_calls_before_a_mask_have_no_faces(lib):
+    m = _model()
+    assert len(m.couple_sample()) == 0
+    assert all(len(a) == 0 for a in m.coupling_faces())
+
+
+def test_batch_submit_checks_every_grid_against_the_dem(lib):
+    b = object.__new__(api.Batch)
+    b._h = api.C.c_void_p(0)
+    b._shapes = {}
+    dem = np.zeros((8, 9))
+    b.submit(dem, depth=np.zeros((8, 9)), manning_classes=np.zeros((8, 9), np.uint8), manning_table=[0.03],
+             rain_weight=np.ones((8, 9), np.float32), rain_mm=[1.0, 2.0])
+    assert lib.calls == ["sw2d_batch_submit"]
+    bad = [dict(depth=np.zeros((9, 8))), dict(manning_classes=np.zeros((8, 8), np.uint8), manning_table=[0.03]),
+           dict(rain_weight=np.ones(72, np.float32))]
+    for kw in bad:
+        with pytest.raises(ValueError):
+            b.submit(dem, **kw)
+    with pytest.raises(ValueError):
+        b.submit(np.zeros(72))
+    assert lib.calls == ["sw2d_batch_submit"]
