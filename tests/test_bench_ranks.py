@@ -75,3 +75,17 @@ def test_reference_arm_line_on_the_cpu():
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["cells"] == 256 * 256
+
+
+def test_cpu_baseline_falls_back_to_the_port(monkeypatch):
+    # without the reference's own CPU build the baseline times the oracle's
+    # restatement of its kernels and says so
+    import bench
+    from oracle import oracle as O
+    sc = bench.workload_config2(128)
+    if O.ref_lib() is not None:
+        v, _, n, kind, _ = bench.cpu_baseline_sample(sc, 3, 1, 2)
+        assert kind == "reference" and n == 3 and v > 0
+    monkeypatch.setattr(O, "ref_lib", lambda: None)
+    v, secs, n, kind, what = bench.cpu_baseline_sample(sc, 3, 1, 2)
+    assert kind == "port" and n == 3 and v > 0 and secs > 0 and "restatement" in what
