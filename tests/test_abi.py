@@ -101,3 +101,20 @@ def test_headers_compile_as_c99_and_link(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.startswith("c-abi ok"), (r.returncode, r.stdout, r.stderr)
+
+
+def test_raster_size_limit_is_checked_before_any_device_call():
+    # 2^30 cells is the largest raster (int cell ids and the padded layouts);
+    # one more row and column is refused as too large, the limit itself
+    # passes the argument checks and fails only for want of a GPU here
+    lib = api.load()
+    h = ctypes.c_void_p()
+    cfg = api.default_config(rows=32769, cols=32769)
+    assert lib.sw2d_create(ctypes.byref(cfg), ctypes.byref(h)) == -1
+    assert b"too large" in lib.sw2d_last_error()
+    # a 1-byte HBM budget: on a machine with a GPU the call stops at the
+    # budget check, before any allocation
+    cfg = api.default_config(rows=32768, cols=32768, hbm_budget_bytes=1.0)
+    rc = lib.sw2d_create(ctypes.byref(cfg), ctypes.byref(h))
+    assert rc in (api.SW2D_ERR_NODEVICE, api.SW2D_ERR_BUDGET), rc
+    assert b"too large" not in lib.sw2d_last_error()
