@@ -393,7 +393,8 @@ def run_batched_leg(args, peak, fp64_value):
     return {"value": round(value, 4), "unit": UNIT, "scenarios": len(specs), "cells": int(cells),
             "steps": args.steps, "ms_per_step": round(ms / args.steps, 4),
             "workload": "batched FP32: %d scenarios, side log-uniform 128-2048, fractal DEM, 3-class Voronoi n, "
-                        "gamma hyetographs, per-scenario CFL length, one fused launch per iteration, "
+                        "gamma hyetographs, per-scenario CFL length, one row-marching launch per iteration "
+                        "(every scenario has a class raster: one feature class) and a finalize, "
                         "256 rows per work item" % len(specs),
             "roofline": {"bound": "hbm", "kernel": "k32_march + k32_finalize", "achieved": round(achieved, 2),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),

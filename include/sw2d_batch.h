@@ -5,8 +5,10 @@
  * after the other (SW2D-EFDC.cu:3733-3738) and calls the step kernels of
  * SW2D-EFDC.cu:97-725 for each.  This interface runs many scenarios of
  * uneven raster sizes together on one GPU: every iteration is one launch of
- * the fused FP32 tile kernel over all running scenarios, each with its own
- * CFL iteration length and forcing.
+ * the FP32 row-marching kernel over all running scenarios of a feature class
+ * (class raster, rain field, ...; one launch per class present) and one
+ * finalize launch, each scenario with its own CFL iteration length and
+ * forcing.
  *
  * Requests are admitted as HBM (the budget given at creation) and running
  * slots free up; their state stays on the device until they reach their end

@@ -1,7 +1,8 @@
 /* Batched and served FP32 SW2D: many scenarios of uneven raster sizes
- * advanced together by the fused tile kernel (one launch per iteration over
- * a work list of (scenario, tile) pairs, each scenario with its own CFL
- * iteration length and forcing), with continuous admission.
+ * advanced together by the row-marching kernel (per iteration, one launch
+ * per feature class present over its part of a work list of (scenario,
+ * strip, row segment) items and one finalize launch; each scenario with its
+ * own CFL iteration length and forcing), with continuous admission.
  *
  * A request is queued on submit with a host copy of its inputs.  Every
  * sw2d_batch_step() admits queued requests (first fit, in arrival order)
@@ -270,7 +271,7 @@ int sw2d_batch_step(sw2d_batch* b, int iterations, int* n_running_out, int* n_qu
         int rc = b->eng->run(iterations, &err);
         if (rc) return bfail(rc, err);
         b->device_ms += b->eng->last_ms();
-        b->launches += 2LL * iterations;
+        b->launches += (long long)iterations * b->eng->launches_per_iteration();
         /* retire finished scenarios (highest index first keeps indices valid) */
         for (size_t k = b->running.size(); k-- > 0;) {
             sw2d::Clock32 c;

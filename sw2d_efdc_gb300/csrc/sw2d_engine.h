@@ -97,6 +97,13 @@ class Engine32 {
     double last_ms() const { return last_ms_; }
     long long last_iters() const { return last_iters_; }
     int nwork() const { return (int)work_.size(); }
+    /* kernel launches of one iteration of the current work list: one
+     * row-marching launch per feature class present, then the finalize */
+    int launches_per_iteration() const {
+        int n = 1;
+        for (int k = 0; k < T32_NCLASS; k++) n += class_n_[k] > 0 ? 1 : 0;
+        return n;
+    }
     int sync(std::string* err);
     /* rows per work item of scenarios added from now on (0 = chosen by
      * segment_rows_for) */
