@@ -368,8 +368,9 @@ def make_batch_specs(n, lo, hi, seed, t_scale=1.0):
 
 
 def run_batched_leg(args, peak, fp64_value):
-    """The batched form: 256 scenarios of uneven size advanced together, one fused
-    launch per iteration (graph-captured chunks), each with its own CFL length."""
+    """The batched form: 256 scenarios of uneven size advanced together, one
+    row-marching launch per feature class and a finalize per iteration
+    (graph-captured chunks), each scenario with its own CFL length."""
     from sw2d_efdc_gb300 import api
     t0 = time.time()
     specs = make_batch_specs(args.batch_n, 128, 2048, 4)
