@@ -1,5 +1,6 @@
 """Device-math helpers (sw2d_math.h) evaluated on the CPU through the oracle
-build: accuracy of the friction power and exactness of constant division."""
+build: accuracy of the friction power, exactness of constant division, the
+clamped series lookup; and the oracle's independence of its thread count."""
 import ctypes
 import os
 import subprocess
@@ -151,3 +152,29 @@ def test_series_index_clamps_beyond_the_int_range():
         assert a.run() == b.run() > 0
         assert np.array_equal(a.fields()["h"], b.fields()["h"])
         assert a.ledger()["source_in"] == 0.0
+
+
+def test_oracle_is_bit_identical_across_thread_counts():
+    # the full-size GPU parity test runs the oracle on every host thread and
+    # compares bit for bit, so its fields and ledger must not depend on the
+    # thread count (CFL maximum, outflow and ledger sums included)
+    from oracle import oracle as O
+    from tests.helpers import bumpy_case
+    rng = np.random.default_rng(41)
+    case = bumpy_case(R=70, C=45, seed=41, dt_mode=O.DT_CFL, cfl=0.7, dt_max=1.0, outflow_south=True,
+                      rain=np.array([15.0, 15.0, 5.0]), dtrain=20.0, t_end=40.0)
+    case.manning_field = rng.choice([0.02, 0.05, 0.1], size=case.dem.shape)
+    case.rain_weight = (0.5 + rng.random(case.dem.shape)).astype(np.float32)
+    runs = []
+    for math in (O.MATH_DEVICE, O.MATH_LIBM):
+        for nt in (1, 3, 8):
+            o = O.Oracle(case, math=math, nthreads=nt)
+            n = o.run()
+            runs.append((math, n, o.fields(), o.ledger()))
+    for math in (O.MATH_DEVICE, O.MATH_LIBM):
+        rs = [r for r in runs if r[0] == math]
+        for _, n, f, led in rs[1:]:
+            assert n == rs[0][1] > 10
+            for k in ("h", "qx", "qy"):
+                assert np.array_equal(f[k], rs[0][2][k]), k
+            assert led == rs[0][3]
