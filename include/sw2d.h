@@ -122,6 +122,11 @@ int sw2d_set_depth(sw2d_handle* h, const double* depth);
  * cells).  The reference has one scalar n (rn, SW2D-EFDC.cu:4810).  NULL
  * classes restores the uniform cfg.manning. */
 int sw2d_set_manning_classes(sw2d_handle* h, const uint8_t* classes, const double* table, int ntable);
+/* Per-cell Manning n as rows*cols values; NULL restores the uniform
+ * cfg.manning.  Stored as the class raster of its distinct values
+ * (sw2d_manning_classes_of), which gives the same face coefficients: at most
+ * 256 distinct values on FP64 handles, 64 on FP32 handles. */
+int sw2d_set_manning_field(sw2d_handle* h, const double* n);
 /* Rain series: n values in mm per dtrain seconds (rain.dat, SW2D-EFDC.cu:4078-4108). */
 int sw2d_set_rain_series(sw2d_handle* h, const double* mm, int n, double dtrain);
 /* Per-cell rain weight (rows*cols floats) multiplying the series rate; NULL = 1. */
@@ -218,6 +223,14 @@ int sw2d_lake_catchment_smooth(int rows, int cols, const int* mask, double* dem)
  * negative values clipped to zero.  Host only. */
 int sw2d_evaporation_series(int n, const double* temp, const double* rad, double albedo, double dtrain,
                             double* mm_out);
+
+/* A per-cell Manning field as classes: table = its distinct values in
+ * ascending order (*ntable_out of them, at most max_classes <= 256),
+ * classes[k] = the index of field[k] in table.  Values must be finite and
+ * >= 0.  SW2D_ERR_INVALID when the field has more than max_classes distinct
+ * values.  Host only. */
+int sw2d_manning_classes_of(int64_t count, const double* field, int max_classes, uint8_t* classes, double* table,
+                            int* ntable_out);
 
 /* Device state snapshot (h, qx, qy, clock, ledger) to a host buffer. */
 int sw2d_snapshot_size(sw2d_handle* h, size_t* bytes);

@@ -95,6 +95,7 @@ SIGNATURES = {
     "sw2d_set_dem": (C.c_int, [C.c_void_p, _dp]),
     "sw2d_set_depth": (C.c_int, [C.c_void_p, _dp]),
     "sw2d_set_manning_classes": (C.c_int, [C.c_void_p, _u8p, _dp, C.c_int]),
+    "sw2d_set_manning_field": (C.c_int, [C.c_void_p, _dp]),
     "sw2d_set_rain_series": (C.c_int, [C.c_void_p, _dp, C.c_int, C.c_double]),
     "sw2d_set_rain_field": (C.c_int, [C.c_void_p, _fp]),
     "sw2d_set_evaporation_series": (C.c_int, [C.c_void_p, _dp, C.c_int]),
@@ -134,6 +135,7 @@ SIGNATURES = {
     "sw2d_lake_catchment_smooth": (C.c_int, [C.c_int, C.c_int, _ip, _dp]),
     "sw2d_test_stall_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "sw2d_evaporation_series": (C.c_int, [C.c_int, _dp, _dp, C.c_double, C.c_double, _dp]),
+    "sw2d_manning_classes_of": (C.c_int, [C.c_int64, _dp, C.c_int, _u8p, _dp, C.POINTER(C.c_int)]),
     "sw2d_measure_state_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                              C.c_void_p, _dp, _dp]),
@@ -227,6 +229,11 @@ class Model:
         tb = np.ascontiguousarray(table, np.float64)
         _check(load().sw2d_set_manning_classes(self._h, _ptr(cl, _u8p), _ptr(tb, _dp), len(tb)),
                "sw2d_set_manning_classes")
+
+    def set_manning_field(self, n):
+        """Per-cell Manning n (rows x cols), or None for the uniform cfg.manning."""
+        n = None if n is None else self._grid(n, np.float64)
+        _check(load().sw2d_set_manning_field(self._h, _ptr(n, _dp)), "sw2d_set_manning_field")
 
     def set_rain_series(self, mm, dtrain):
         mm = np.ascontiguousarray(mm, np.float64)
@@ -539,3 +546,16 @@ def evaporation_series(temp, rad, albedo, dtrain):
     _check(load().sw2d_evaporation_series(len(T), _ptr(T, _dp), _ptr(Rg, _dp), float(albedo), float(dtrain),
                                           _ptr(out, _dp)), "sw2d_evaporation_series")
     return out
+
+
+def manning_classes_of(field, max_classes=256):
+    """A per-cell Manning field as (classes, table): table = its distinct values
+    in ascending order, classes = each cell's index into it (uint8, the
+    field's shape)."""
+    f = np.ascontiguousarray(field, np.float64)
+    cls = np.zeros(f.shape, np.uint8)
+    table = np.zeros(256)
+    nt = C.c_int(0)
+    _check(load().sw2d_manning_classes_of(f.size, _ptr(f, _dp), int(max_classes), _ptr(cls, _u8p),
+                                          _ptr(table, _dp), C.byref(nt)), "sw2d_manning_classes_of")
+    return cls, table[:nt.value].copy()

@@ -863,6 +863,18 @@ int sw2d_set_manning_classes(sw2d_handle* h, const uint8_t* cls, const double* t
     return SW2D_OK;
 }
 
+int sw2d_set_manning_field(sw2d_handle* h, const double* n) {
+    if (!h) return fail(SW2D_ERR_INVALID, "null handle");
+    if (!n) return sw2d_set_manning_classes(h, nullptr, nullptr, 0);
+    const int64_t cells = (int64_t)h->R * h->C;
+    std::vector<uint8_t> cls((size_t)cells);
+    double table[256];
+    int ntable = 0;
+    int rc = sw2d_manning_classes_of(cells, n, h->fp32() ? 64 : 256, cls.data(), table, &ntable);
+    if (rc) return rc;
+    return sw2d_set_manning_classes(h, cls.data(), table, ntable);
+}
+
 int sw2d_set_rain_series(sw2d_handle* h, const double* mm, int n, double dtrain) {
     if (!h || (n > 0 && !mm) || n < 0 || !(dtrain > 0)) return fail(SW2D_ERR_INVALID, "rain series");
     if (h->fp32()) {

@@ -3,9 +3,11 @@
  *  - sw2d_lake_catchment_smooth: the DEM pre-pass of a coupled run
  *    (lake_catchment_smooth, SW2D-EFDC.cu:2766-2827);
  *  - sw2d_evaporation_series: the evaporation series from temperature and
- *    radiation (gpu_evaporation_calc, SW2D-EFDC.cu:556-586).
+ *    radiation (gpu_evaporation_calc, SW2D-EFDC.cu:556-586);
+ *  - sw2d_manning_classes_of: a per-cell Manning field as a class raster and
+ *    the table of its distinct values (the reference has one scalar n).
  *
- * Both run once per case over at most rows*cols values.  The smoothing pass
+ * All run once per case over at most rows*cols values.  The smoothing pass
  * stays on the host because its result depends on its sweep order: each
  * cell reads the already-updated cells south and west of it, so a device
  * version would need a wavefront of rows+cols dependent steps for a pass
@@ -15,7 +17,11 @@
  */
 #include "sw2d.h"
 
+#include <algorithm>
+#include <cmath>
 #include <cstddef>
+#include <string>
+#include <vector>
 
 namespace sw2d {
 void set_error_message(const char* msg); /* sw2d_api.cu */
@@ -74,5 +80,27 @@ extern "C" int sw2d_evaporation_series(int n, const double* temp, const double* 
         const double e = (rs / (lv * pw)) * dtrain * 1000.0;
         mm_out[i] = e < 0 ? 0 : e;
     }
+    return SW2D_OK;
+}
+
+extern "C" int sw2d_manning_classes_of(int64_t count, const double* field, int max_classes, uint8_t* classes,
+                                       double* table, int* ntable_out) {
+    if (count < 0 || max_classes < 1 || max_classes > 256) return bad("count >= 0, 1 <= max_classes <= 256");
+    if (count > 0 && (!field || !classes || !table)) return bad("null argument");
+    std::vector<double> v(field, field + count);
+    for (double x : v)
+        if (!(x >= 0) || !std::isfinite(x)) return bad("Manning n must be finite and >= 0");
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    if ((int64_t)v.size() > max_classes) {
+        sw2d::set_error_message(("Manning field has " + std::to_string(v.size()) + " distinct values, at most " +
+                                 std::to_string(max_classes) + " fit the class table")
+                                    .c_str());
+        return SW2D_ERR_INVALID;
+    }
+    for (int64_t k = 0; k < count; k++)
+        classes[k] = (uint8_t)(std::lower_bound(v.begin(), v.end(), field[k]) - v.begin());
+    std::copy(v.begin(), v.end(), table);
+    if (ntable_out) *ntable_out = (int)v.size();
     return SW2D_OK;
 }

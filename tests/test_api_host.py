@@ -1,6 +1,8 @@
-"""Host-side argument checks of the Python mirror (api.py) on the CPU: the C
-ABI cannot know the length of a host array, so shapes are checked before
-any call reaches the library.  A recording stand-in replaces the library."""
+"""Host-side parts of the library and its Python mirror on the CPU: the
+mirror's argument checks (the C ABI cannot know the length of a host array,
+so shapes are checked before any call reaches the library; a recording
+stand-in replaces the library in the tests that take the `lib` fixture) and
+the host-only Manning class helper (the real library)."""
 import numpy as np
 import pytest
 
@@ -76,3 +78,37 @@ def test_batch_submit_checks_every_grid_against_the_dem(lib):
     with pytest.raises(ValueError):
         b.submit(np.zeros(72))
     assert lib.calls == ["sw2d_batch_submit"]
+
+
+def test_manning_classes_of_matches_numpy_unique():
+    rng = np.random.default_rng(3)
+    for shape, k in (((40, 30), 3), ((7, 11), 256), ((1, 1), 1), ((64, 64), 64)):
+        values = np.sort(rng.uniform(0.01, 0.2, k))
+        field = rng.choice(values, size=shape)
+        cls, table = api.manning_classes_of(field)
+        ref_table, ref_cls = np.unique(field, return_inverse=True)
+        assert np.array_equal(table, ref_table)
+        assert np.array_equal(cls, ref_cls.reshape(shape).astype(np.uint8))
+        assert np.array_equal(table[cls], field)  # the round trip is exact
+
+
+def test_manning_classes_of_refuses_what_a_table_cannot_hold():
+    field = np.linspace(0.01, 0.2, 300)
+    with pytest.raises(api.Sw2dError) as e:
+        api.manning_classes_of(field)
+    assert "300 distinct values" in str(e.value)
+    with pytest.raises(api.Sw2dError):
+        api.manning_classes_of(field[:65], max_classes=64)
+    api.manning_classes_of(field[:64], max_classes=64)
+    for bad in (np.nan, -0.01, np.inf):
+        with pytest.raises(api.Sw2dError):
+            api.manning_classes_of(np.array([0.03, bad]))
+
+
+def test_manning_field_shape_is_checked(lib):
+    m = _model()
+    m.set_manning_field(np.full((6, 5), 0.03))
+    m.set_manning_field(None)
+    with pytest.raises(ValueError):
+        m.set_manning_field(np.full((5, 6), 0.03))
+    assert lib.calls == ["sw2d_set_manning_field"] * 2
