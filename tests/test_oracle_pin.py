@@ -207,3 +207,34 @@ def test_pin_random_cases_with_sources_and_evaporation(seed):
         case.evap = api.evaporation_series(T, Rg, albedo, dtrain)
         kw["evap_inputs"] = (T, Rg, albedo)
     _pin(case, **kw)
+
+
+@pytest.mark.parametrize("kind", ["all_nodata", "dry_no_rain", "all_wet", "one_active_cell"])
+def test_pin_degenerate_rasters(kind):
+    R, C = 12, 9
+    rng = np.random.default_rng(77)
+    dem = 0.01 * np.arange(R)[::-1, None] + 0.02 * rng.standard_normal((R, C))
+    h0 = np.zeros((R, C))
+    rain = np.array([8.0, 8.0, 8.0])
+    if kind == "all_nodata":
+        dem[:] = -9999.0
+    elif kind == "dry_no_rain":
+        rain = np.zeros(3)
+    elif kind == "all_wet":
+        h0[:] = 0.5 + 0.1 * rng.random((R, C))
+    else:
+        dem[:] = -9999.0
+        dem[R // 2, C // 2] = 1.0
+        h0[R // 2, C // 2] = 0.3
+    case = O.Case(dem=dem, h0=h0, cellsize=2.0, manning=0.03, dt=0.02, t_end=3.0, rain=rain, dtrain=1.3)
+    o, ref = _pin(case)
+    if kind in ("all_nodata", "dry_no_rain"):
+        assert not ref["h"].any()
+    if kind == "one_active_cell":
+        # nothing flows out of a cell walled in by NODATA: its volume changes
+        # by the rain alone (negative after 2.6 s, where the reference's
+        # interpolation divides the step to the series' zero tail by the
+        # elapsed time)
+        led = o.ledger()
+        assert abs(led["volume"] - 0.3 * 4.0 - led["rain_in"]) < 1e-12
+        assert led["outflow"] == 0.0
