@@ -83,13 +83,10 @@ def test_pin_point_sources():
     _pin(case, sources=(brx, bry, qq, dtoq, 0.0, 0.0))
 
 
-def test_pin_coupling_samples():
-    case = bumpy_case(R=34, C=30, seed=15, holes=False, t_end=9.0, dt=0.05)
-    mask = np.zeros(case.dem.shape, np.int32)
-    mask[10:20, 8:22] = 1
-    mask[0:2, 12:16] = 1
-    lkout = 20
-    max_samples = 16
+def _pin_coupling(case, mask, lkout, max_samples):
+    """The reference's face lists and samples (couple_BC_efdc through its own
+    loop, with the velocity of the previous output) against the oracle's face
+    scan and sample rule replayed on the oracle's fields."""
     ref = O.run_reference(case, nthreads=2, mask=mask, lkout=lkout, efdc_basetime=3600.0,
                           max_samples=max_samples)
     side, ci, cj, cell = O.couple_faces(mask)
@@ -103,7 +100,6 @@ def test_pin_coupling_samples():
     # replay the samples with the oracle and the reference's lag
     o = O.Oracle(case, math=O.MATH_LIBM)
     prev = None
-    t = 0
     mstep = 0
     tq = -1
     first = True
@@ -123,7 +119,33 @@ def test_pin_coupling_samples():
                 assert np.array_equal(ref["val"][s][tq][1:nb + 1], q[sel]), (tq, s)
             prev = f
             first = False
-    assert tq + 1 == ref["nsamples"] > 3
+    assert tq + 1 == ref["nsamples"]
+    return len(side), ref["nsamples"]
+
+
+def test_pin_coupling_samples():
+    case = bumpy_case(R=34, C=30, seed=15, holes=False, t_end=9.0, dt=0.05)
+    mask = np.zeros(case.dem.shape, np.int32)
+    mask[10:20, 8:22] = 1
+    mask[0:2, 12:16] = 1
+    nfaces, nsamples = _pin_coupling(case, mask, lkout=20, max_samples=16)
+    assert nfaces > 0 and nsamples > 3
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_pin_coupling_random_masks(seed):
+    # one to three lake blobs anywhere, edges and corners included, on a
+    # raster with ponds and rain
+    rng = np.random.default_rng(3000 + seed)
+    R, C = int(rng.integers(8, 30)), int(rng.integers(8, 30))
+    case = bumpy_case(R=max(R, 21), C=max(C, 15), seed=seed, holes=False, t_end=2.0, dt=0.05)
+    R, C = case.dem.shape
+    mask = np.zeros((R, C), np.int32)
+    for _ in range(int(rng.integers(1, 4))):
+        r0, c0 = int(rng.integers(0, R - 1)), int(rng.integers(0, C - 1))
+        mask[r0:r0 + int(rng.integers(1, 8)), c0:c0 + int(rng.integers(1, 8))] = 1
+    nfaces, nsamples = _pin_coupling(case, mask, lkout=int(rng.choice([2, 4, 10])), max_samples=64)
+    assert nsamples >= 2
 
 
 def test_device_math_flavour_tracks_the_reference_flavour_on_long_runs():
