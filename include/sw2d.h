@@ -175,6 +175,11 @@ int sw2d_set_coupling_mask(sw2d_handle* h, const int* mask, int lagged, int* n_f
 /* Face list: side (0 north, 1 south, 2 east, 3 west as the reference's
  * north_bc..west_bc arrays), EFDC I and J (1-based), raster cell id. */
 int sw2d_get_coupling_faces(sw2d_handle* h, int* side, int* efdc_i, int* efdc_j, int* cell, int capacity);
+/* The same face list for a lake mask (rows*cols, 1 = lake) without a handle:
+ * *n_out faces, the first `capacity` of them written (any output may be
+ * NULL).  Host only. */
+int sw2d_coupling_faces_of(int rows, int cols, const int* mask, int* side, int* efdc_i, int* efdc_j, int* cell,
+                           int capacity, int* n_out);
 /* Take one coupling sample at the current state; when initial is nonzero the
  * depths are the initial condition and the velocities zero, as the
  * reference's first sample (SW2D-EFDC.cu:4905).  q_out: n_faces discharges

@@ -136,6 +136,7 @@ SIGNATURES = {
     "sw2d_test_stall_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "sw2d_evaporation_series": (C.c_int, [C.c_int, _dp, _dp, C.c_double, C.c_double, _dp]),
     "sw2d_manning_classes_of": (C.c_int, [C.c_int64, _dp, C.c_int, _u8p, _dp, C.POINTER(C.c_int)]),
+    "sw2d_coupling_faces_of": (C.c_int, [C.c_int, C.c_int, _ip, _ip, _ip, _ip, _ip, C.c_int, C.POINTER(C.c_int)]),
     "sw2d_measure_state_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                              C.c_void_p, _dp, _dp]),
@@ -559,3 +560,19 @@ def manning_classes_of(field, max_classes=256):
     _check(load().sw2d_manning_classes_of(f.size, _ptr(f, _dp), int(max_classes), _ptr(cls, _u8p),
                                           _ptr(table, _dp), C.byref(nt)), "sw2d_manning_classes_of")
     return cls, table[:nt.value].copy()
+
+
+def coupling_faces_of(mask):
+    """The boundary faces of a lake mask (rows x cols, 1 = lake) in the
+    reference's scan order, as Model.coupling_faces returns them: (side,
+    EFDC I, EFDC J, raster cell), without a handle."""
+    m = np.ascontiguousarray(mask, np.int32)
+    if m.ndim != 2:
+        raise ValueError("mask must be a (rows, cols) array")
+    n = C.c_int(0)
+    _check(load().sw2d_coupling_faces_of(m.shape[0], m.shape[1], _ptr(m, _ip), None, None, None, None, 0,
+                                         C.byref(n)), "sw2d_coupling_faces_of")
+    out = [np.zeros(n.value, np.int32) for _ in range(4)]
+    _check(load().sw2d_coupling_faces_of(m.shape[0], m.shape[1], _ptr(m, _ip), *(_ptr(a, _ip) for a in out),
+                                         n.value, C.byref(n)), "sw2d_coupling_faces_of")
+    return tuple(out)

@@ -1323,23 +1323,25 @@ int sw2d_test_stall_staging(sw2d_handle* h, int on) {
 
 /* ---------------- coupling: SW2D-EFDC.cu:728-1067 ---------------------- */
 
-int sw2d_set_coupling_mask(sw2d_handle* h, const int* mask, int lagged, int* n_faces_out) {
-    if (!h || !mask) return fail(SW2D_ERR_INVALID, "null argument");
-    int rc = set_device(h);
-    if (rc) return rc;
-    const int rows = h->R, cols = h->C;
-    h->f_side.clear();
-    h->f_i.clear();
-    h->f_j.clear();
-    h->f_cell.clear();
+}  /* extern "C" */
+
+/* The boundary faces of a lake mask (1 = lake) as couple_BC_efdc finds them
+ * (SW2D-EFDC.cu:739-1065): rows from the bottom (ini), columns left to
+ * right, each non-lake cell testing south, north, east, west in that order;
+ * edge rows and columns test only the sides the reference tests there,
+ * corner cells none.  Side 0 N, 1 S, 2 E, 3 W; EFDC 1-based (I, J). */
+static void scan_coupling_faces(int rows, int cols, const int* mask, std::vector<int>* side, std::vector<int>* fi,
+                                std::vector<int>* fj, std::vector<int>* cell) {
+    side->clear();
+    fi->clear();
+    fj->clear();
+    cell->clear();
     auto add = [&](int sd, int i, int j, int p) {
-        h->f_side.push_back(sd);
-        h->f_i.push_back(i);
-        h->f_j.push_back(j);
-        h->f_cell.push_back(p);
+        side->push_back(sd);
+        fi->push_back(i);
+        fj->push_back(j);
+        cell->push_back(p);
     };
-    /* the reference scans rows from the bottom (ini) and columns left to right,
-     * testing south, north, east, west in that order */
     for (int ini = 0; ini < rows; ini++) {
         int base = rows * cols - (ini + 1) * cols;
         for (int inj = 0; inj < cols; inj++) {
@@ -1361,6 +1363,33 @@ int sw2d_set_coupling_mask(sw2d_handle* h, const int* mask, int lagged, int* n_f
             if (W && mask[p] != mask[p + 1]) add(3, inj + 2, ini + 1, p);
         }
     }
+}
+
+extern "C" {
+
+int sw2d_coupling_faces_of(int rows, int cols, const int* mask, int* side, int* efdc_i, int* efdc_j, int* cell,
+                           int capacity, int* n_out) {
+    if (!mask || rows < 1 || cols < 1 || capacity < 0) return fail(SW2D_ERR_INVALID, "invalid argument");
+    if ((long long)rows * cols > (1LL << 30)) return fail(SW2D_ERR_INVALID, "raster too large");
+    std::vector<int> sd, fi, fj, fc;
+    scan_coupling_faces(rows, cols, mask, &sd, &fi, &fj, &fc);
+    const int n = (int)sd.size();
+    for (int k = 0; k < std::min(n, capacity); k++) {
+        if (side) side[k] = sd[k];
+        if (efdc_i) efdc_i[k] = fi[k];
+        if (efdc_j) efdc_j[k] = fj[k];
+        if (cell) cell[k] = fc[k];
+    }
+    if (n_out) *n_out = n;
+    return SW2D_OK;
+}
+
+int sw2d_set_coupling_mask(sw2d_handle* h, const int* mask, int lagged, int* n_faces_out) {
+    if (!h || !mask) return fail(SW2D_ERR_INVALID, "null argument");
+    int rc = set_device(h);
+    if (rc) return rc;
+    const int cols = h->C;
+    scan_coupling_faces(h->R, h->C, mask, &h->f_side, &h->f_i, &h->f_j, &h->f_cell);
     h->nfaces = (int)h->f_side.size();
     h->lagged = lagged ? 1 : 0;
     if (h->fp32()) {

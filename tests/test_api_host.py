@@ -112,3 +112,17 @@ def test_manning_field_shape_is_checked(lib):
     with pytest.raises(ValueError):
         m.set_manning_field(np.full((5, 6), 0.03))
     assert lib.calls == ["sw2d_set_manning_field"] * 2
+
+
+def test_coupling_faces_of_edge_cases():
+    # no lake: no faces; all lake: no faces (only non-lake cells test sides);
+    # a lake cell in a corner: its neighbours on the edges see it only along
+    # the sides the reference tests there
+    assert all(len(a) == 0 for a in api.coupling_faces_of(np.zeros((5, 6), np.int32)))
+    assert all(len(a) == 0 for a in api.coupling_faces_of(np.ones((5, 6), np.int32)))
+    m = np.zeros((5, 6), np.int32)
+    m[0, 0] = 1
+    side, fi, fj, cell = api.coupling_faces_of(m)
+    assert len(side) == 2 and sorted(cell.tolist()) == [1, 6]
+    with pytest.raises(api.Sw2dError):
+        api.coupling_faces_of(np.zeros((0, 4), np.int32))

@@ -260,3 +260,27 @@ def test_pin_degenerate_rasters(kind):
         led = o.ledger()
         assert abs(led["volume"] - 0.3 * 4.0 - led["rain_in"]) < 1e-12
         assert led["outflow"] == 0.0
+
+
+@pytest.mark.parametrize("seed", range(30))
+def test_library_face_scan_matches_the_reference(seed):
+    # the library's own scan (the one sw2d_set_coupling_mask runs) on random
+    # masks, edges and corners included, against the reference's face arrays
+    from sw2d_efdc_gb300 import api
+    rng = np.random.default_rng(4000 + seed)
+    R, C = int(rng.integers(21, 40)), int(rng.integers(15, 40))
+    mask = (rng.random((R, C)) < rng.uniform(0.05, 0.6)).astype(np.int32)
+    if seed % 3 == 0:
+        mask[:, :] = 0
+        r0, c0 = int(rng.integers(0, R - 3)), int(rng.integers(0, C - 3))
+        mask[r0:r0 + int(rng.integers(2, 12)), c0:c0 + int(rng.integers(2, 12))] = 1
+    side, fi, fj, cell = api.coupling_faces_of(mask)
+    for got, want in zip((side, fi, fj, cell), O.couple_faces(mask)):
+        assert np.array_equal(got, want)
+    case = bumpy_case(R=R, C=C, seed=seed, holes=False, t_end=0.3, dt=0.05)
+    ref = O.run_reference(case, nthreads=1, mask=mask, lkout=2, efdc_basetime=3600.0, max_samples=4)
+    for s in range(4):
+        sel = side == s
+        nb = int(sel.sum())
+        assert np.array_equal(ref["bc"][s][:nb], np.stack([fi[sel], fj[sel], np.arange(1, nb + 1)], axis=1))
+        assert not ref["bc"][s][nb:].any()
