@@ -175,3 +175,33 @@ def test_evaporation_series_matches_the_reference():
         got = api.evaporation_series(T, Rg, albedo, dtrain)
         assert got.tobytes() == ref.tobytes()
         assert (got >= 0).all() and (got[Rg < 0] == 0).all()
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_cards_match_the_reference_writer_on_random_masks(tmp_path, seed):
+    L = O.ref_lib()
+    if L is None:
+        pytest.skip("reference CPU build unavailable")
+    rng = np.random.default_rng(500 + seed)
+    R, C = int(rng.integers(21, 36)), int(rng.integers(15, 36))
+    case = bumpy_case(R=R, C=C, seed=seed, holes=False, t_end=0.3, dt=0.05)
+    mask = np.zeros((R, C), np.int32)
+    for _ in range(int(rng.integers(1, 4))):
+        r0, c0 = int(rng.integers(0, R - 2)), int(rng.integers(0, C - 2))
+        mask[r0:r0 + int(rng.integers(2, 10)), c0:c0 + int(rng.integers(2, 10))] = 1
+    ref = O.run_reference(case, nthreads=1, mask=mask, lkout=2, efdc_basetime=3600.0, max_samples=4)
+    side, fi, fj, _ = api.coupling_faces_of(mask)
+    n = len(side)
+    assert n == ref["nqs"]
+    bc = np.ascontiguousarray(ref["bc"], np.int32)
+    salt, temp, dye = (int(v) for v in rng.integers(0, 2, 3))
+    tpl = _template(rng.choice(["\n", "\r\n"]), rows=int(rng.integers(0, 60)))
+    a, b = tmp_path / "ref_EFDC.INP", tmp_path / "EFDC.INP"
+    a.write_bytes(tpl)
+    b.write_bytes(tpl)
+    L.sw2dref_write_config.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    assert L.sw2dref_write_config(os.fsencode(a), bc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                  ref["water_cells"], n, 3, salt, temp, dye) == 0
+    api.write_efdc_cards(b, side, fi, fj, salt_on=salt, temp_on=temp, dye_on=dye)
+    assert _region(a.read_bytes()) == _region(b.read_bytes())
