@@ -82,3 +82,42 @@ def test_concentration_decks_match_the_reference_writers(tmp_path, kind, nlayers
     b_path = tmp_path / ("%sSER.INP" % kind)
     api.write_efdc_concentration(b_path, kind, side, val[0, :ns, 0], value, type=0, nlayers=nlayers)
     assert a.read_bytes() == b_path.read_bytes()
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_qser_matches_the_reference_writer_on_random_runs(tmp_path, seed):
+    # random lake masks, sample intervals, layer counts, deck types and base
+    # times; the samples are the reference's own from its coupling run
+    L = O.ref_lib()
+    if L is None:
+        pytest.skip("reference CPU build unavailable")
+    rng = np.random.default_rng(700 + seed)
+    R, C = int(rng.integers(21, 36)), int(rng.integers(15, 36))
+    case = bumpy_case(R=R, C=C, seed=seed, holes=False, t_end=float(rng.uniform(1.0, 4.0)), dt=0.05)
+    mask = np.zeros((R, C), np.int32)
+    for _ in range(int(rng.integers(1, 4))):
+        r0, c0 = int(rng.integers(0, R - 2)), int(rng.integers(0, C - 2))
+        mask[r0:r0 + int(rng.integers(2, 10)), c0:c0 + int(rng.integers(2, 10))] = 1
+    basetime = float(rng.choice([60.0, 3600.0, 86400.0]))
+    max_samples = 64
+    ref = O.run_reference(case, nthreads=1, mask=mask, lkout=int(rng.choice([2, 6, 10])), efdc_basetime=basetime,
+                          max_samples=max_samples)
+    wc, ns = ref["water_cells"], ref["nsamples"]
+    bc = np.ascontiguousarray(ref["bc"], np.int32)
+    val = np.ascontiguousarray(ref["val"], np.float64)
+    nlayers, dtype = int(rng.integers(1, 5)), int(rng.integers(0, 2))
+    L.sw2dref_write_qser.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                     ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_int]
+    a = tmp_path / "ref_QSER.INP"
+    assert L.sw2dref_write_qser(os.fsencode(a), dtype, nlayers, bc.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                val.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), wc, max_samples, basetime,
+                                ns) == 0
+    side, fi, fj, cell = api.coupling_faces_of(mask)
+    q = np.zeros((ns, len(side)))
+    for s in range(4):
+        for b, k in enumerate(np.flatnonzero(side == s), start=1):
+            q[:, k] = val[s, :ns, b]
+    b_path = tmp_path / "QSER.INP"
+    api.write_qser(b_path, side, val[0, :ns, 0], q, type=dtype, nlayers=nlayers, efdc_basetime=basetime)
+    assert a.read_bytes() == b_path.read_bytes()
