@@ -39,12 +39,11 @@ BYTES_PER_CELL_FP64_CFG2 = 62  # h,qx,qy r+w 48 + z 8 + flag 1 + Manning class 1
 BYTES_PER_CELL_K64_FLUX = 66
 # DRAM bytes per cell of one k64_flux launch, 4096 x 4096 pond-break at t = 600 s: ncu
 # dram__bytes_read.sum + dram__bytes_write.sum = 821.7 + 251.0 MB over 16.78 M cells
-# (profiles/k64_flux_4096.md)
 TRAFFIC_PER_CELL_K64_FLUX = 63.93
 BYTES_PER_CELL_FP32_CFG3 = 37  # h,qx,qy r+w 24 + z offset 4 + info byte 1 + Kahan compensation r+w 8
 # DRAM bytes per cell of one k32_march launch, 4096 x 4096 precision form at t = 1200 s: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum = 360.3 + 221.8 MB over 16.78 M cells
-# (profiles/k32_march_4096.md); the launch streams every field once, so the figure scales with cells
+# dram__bytes_read.sum + dram__bytes_write.sum = 360.3 + 221.8 MB over 16.78 M cells; the
+# launch streams every field once, so the figure scales with cells
 TRAFFIC_PER_CELL_K32_MARCH = 34.69
 
 
@@ -262,8 +261,8 @@ def run_fp32_leg(args, peak):
     m.set_depth(sc.h0)
     m.advance(args.fp32_spinup_s)
     t_spun = m.time()[0]
-    K = args.steps + (args.steps & 1)
-    m.step(max(args.warmup, 3))
+    K = args.steps
+    m.step(args.warmup)
     with TimedRegion(args.profile_timed):
         m.step(K)
     ms_iter, _ = m.timing()
@@ -287,32 +286,83 @@ def run_fp32_leg(args, peak):
     }
 
 
-def run_precision_leg(args):
-    """Errors of the FP32 precision form against the FP64 path (itself
-    bit-identical to the oracle) on the 8192 x 8192 generator at a raster the
-    FP64 path finishes in seconds: peak depth per cell, outlet peak discharge
-    and its time, flood arrival time per cell (first sample with h > 1 cm)
-    and the volume balance of both runs."""
+def run_config1_leg(args):
+    """The 256 x 256 plain FP64 workload (dx 10 m, 1 % plane + bumps, n 0.03,
+    dry bed, 50 mm/h for 30 min, free south outlet, CFL 0.7) over its whole
+    simulated hour: the FP64 path through the C ABI, device-timed, and the
+    oracle's restatement of the reference's kernels (its libm flavour, bit
+    for bit the reference's own arithmetic, with the CFL rule and the outlet
+    the reference lacks) on all host cores, the B1 line of this workload."""
+    from oracle import oracle as O
     from sw2d_efdc_gb300 import api, synth
-    size, T, dts = args.prec_size, args.prec_t, args.prec_sample
-    sc = synth.config3(rows=size, cols=size)
+    sc = synth.config1()
+    cells = sc.rows * sc.cols
+    m = make_model(sc)
+    load_inputs(m, sc)
+    m.set_outlet_record(1 << 16)
+    w0 = time.perf_counter()
+    n = m.advance(sc.t_end)
+    wall = time.perf_counter() - w0
+    ms_iter, _ = m.timing()
+    h = m.depth()
+    _, q = m.outlet()
+    led = m.ledger()
+    m.close()
+    gpu = cells * n / (ms_iter * 1e-3 * n) / 1e9
+    out = {"workload": "plain FP64 256x256 dx=10m, 1%% plane + Gaussian bumps (sigma 0.3 m, corr 50 m), n 0.03, "
+                       "dry bed, 50 mm/h for 30 min, free south outlet, CFL 0.7, th 1e-4, %.0f s simulated" % sc.t_end,
+           "iterations": int(n), "value": round(gpu, 4), "unit": UNIT,
+           "device_ms_per_iteration": round(ms_iter, 5), "run_wall_s": round(wall, 3),
+           "outlet_peak_q_m3s": float(q.max()) if len(q) else 0.0, "balance_error": led["balance_error"]}
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        case = O.Case(dem=sc.dem, h0=sc.h0, cellsize=sc.dx, manning=sc.manning, rain=np.asarray(sc.rain_mm),
+                      dtrain=sc.dtrain, rain_mode=O.RAIN_STEP, dt_mode=O.DT_CFL, cfl=sc.cfl, dt_max=sc.dt_max,
+                      outflow_south=True, t_end=sc.t_end)
+        o = O.Oracle(case, math=O.MATH_LIBM, nthreads=threads)
+        t0 = time.perf_counter()
+        no = o.run()
+        secs = time.perf_counter() - t0
+        hl = o.fields()["h"]
+        o.close()
+        out["cpu_baseline"] = {"value": round(cells * no / secs / 1e9, 5), "unit": UNIT, "cores": threads,
+                               "kind": "port", "run_s": round(secs, 3), "iterations": int(no),
+                               "sample": "the whole 1 h run, the oracle's C restatement of the reference's kernels "
+                                         "(libm flavour) with the CFL rule and free outlet"}
+        out["max_dh_vs_reference_flavour_m"] = float(np.abs(h - hl).max())
+        out["wet_dry_threshold_ties"] = int(((h > 1e-4) != (hl > 1e-4)).sum())
+        out["vs_cpu"] = round(out["value"] / out["cpu_baseline"]["value"], 2)
+    return out
+
+
+PREC_TOL_M = 1e-3  # peak-depth tolerance of the precision form (1 mm)
+
+
+def precision_runs(size, T, dts, members, dev=0, seed=3):
+    """Runs of the precision-form workload (the 8192 x 8192 generator, dx 1 m,
+    1 % plane + bumps, gamma 5-min hyetograph) at `size` x `size` for T
+    simulated seconds, each sampled every dts seconds: peak depth per cell,
+    flood arrival per cell (first sample with h > 1 cm), outlet hydrograph,
+    ledger.  members: (name, precision, rain scale, DEM noise amplitude in m)."""
+    from sw2d_efdc_gb300 import api, synth
+    sc = synth.config3(rows=size, cols=size, seed=seed)
     res = {}
-    # the FP64 run once more with the rain scaled by (1 + 1e-6): the spread
-    # the model itself shows for an input change far below any measurement
-    # error, against which the FP32 errors are read
-    for key, prec, rscale in (("fp64", api.FP64, 1.0), ("fp64_perturbed", api.FP64, 1.0 + 1e-6),
-                              ("fp32", api.FP32, 1.0)):
-        cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=prec, dt_mode=sc.dt_mode, device=device(),
+    for key, prec, rscale, dz in members:
+        cfg = api.default_config(rows=sc.rows, cols=sc.cols, precision=prec, dt_mode=sc.dt_mode, device=dev,
                                  series_mode=sc.series_mode, dx=sc.dx, dy=sc.dx, manning=sc.manning, cfl=sc.cfl,
                                  dt_max=sc.dt_max, outflow=api.OUTFLOW_SOUTH)
         m = api.Model(cfg)
-        m.set_dem(sc.dem)
+        dem = sc.dem
+        if dz:
+            dem = dem + np.random.default_rng(17).uniform(-dz, dz, dem.shape)
+        m.set_dem(dem)
         m.set_rain_series(np.asarray(sc.rain_mm) * rscale, sc.dtrain)
         m.set_depth(sc.h0)
-        m.set_outlet_record(1 << 20)
+        m.set_outlet_record(1 << 21)
         peak = np.zeros((sc.rows, sc.cols))
         arrival = np.full((sc.rows, sc.cols), np.inf)
         t = 0.0
+        w0 = time.perf_counter()
         while t < T:
             t = min(T, t + dts)
             m.advance(t)
@@ -320,35 +370,88 @@ def run_precision_leg(args):
             np.maximum(peak, h, out=peak)
             arrival[(h > 0.01) & np.isinf(arrival)] = t
         tq, q = m.outlet()
-        res[key] = {"peak": peak, "arrival": arrival, "tq": tq, "q": q, "ledger": m.ledger(), "iters": m.time()[1]}
+        res[key] = {"peak": peak, "arrival": arrival, "tq": tq, "q": q, "ledger": m.ledger(),
+                    "iters": m.time()[1], "wall_s": time.perf_counter() - w0}
         m.close()
+    return sc, res
 
-    def errors(a, b):
-        dpk = np.abs(a["peak"] - b["peak"])
-        both = np.isfinite(a["arrival"]) & np.isfinite(b["arrival"])
-        darr = np.abs(a["arrival"][both] - b["arrival"][both])
-        ia, ib = int(np.argmax(a["q"])), int(np.argmax(b["q"]))
-        qa, qb = float(a["q"][ia]), float(b["q"][ib])
-        return {"peak_depth_err_max_m": float(dpk.max()), "peak_depth_err_p99_m": float(np.percentile(dpk, 99)),
-                "peak_depth_err_p999_m": float(np.percentile(dpk, 99.9)), "cells_peak_err_over_1mm": int((dpk > 1e-3).sum()),
-                "outlet_peak_q_rel_err": abs(qb - qa) / max(abs(qa), 1e-300),
-                "outlet_peak_time_err_s": abs(float(b["tq"][ib]) - float(a["tq"][ia])),
-                "arrival_err_max_s": float(darr.max()) if darr.size else 0.0,
-                "arrival_err_mean_s": float(darr.mean()) if darr.size else 0.0,
-                "arrival_cells_in_one_only": int((np.isfinite(a["arrival"]) != np.isfinite(b["arrival"])).sum())}
 
+def precision_errors(a, b, tol=PREC_TOL_M):
+    """Errors of run b against run a (peak depth per cell, outlet peak, arrival)."""
+    dpk = np.abs(a["peak"] - b["peak"])
+    both = np.isfinite(a["arrival"]) & np.isfinite(b["arrival"])
+    darr = np.abs(a["arrival"][both] - b["arrival"][both])
+    ia, ib = int(np.argmax(a["q"])), int(np.argmax(b["q"]))
+    qa, qb = float(a["q"][ia]), float(b["q"][ib])
+    return {"peak_depth_err_max_m": float(dpk.max()), "peak_depth_err_p99_m": float(np.percentile(dpk, 99)),
+            "peak_depth_err_p999_m": float(np.percentile(dpk, 99.9)),
+            "cells_peak_err_over_tol": int((dpk > tol).sum()),
+            "outlet_peak_q_rel_err": abs(qb - qa) / max(abs(qa), 1e-300),
+            "outlet_peak_time_err_s": abs(float(b["tq"][ib]) - float(a["tq"][ia])),
+            "arrival_err_max_s": float(darr.max()) if darr.size else 0.0,
+            "arrival_err_mean_s": float(darr.mean()) if darr.size else 0.0,
+            "arrival_cells_in_one_only": int((np.isfinite(a["arrival"]) != np.isfinite(b["arrival"])).sum())}
+
+
+def fp32_only_cells(res, tol=PREC_TOL_M, base="fp64", fp32="fp32"):
+    """The cells where the FP32 form's peak depth is off by more than tol
+    although no perturbed FP64 run moves that cell's peak by more than tol:
+    errors the model's own conditioning does not explain.  Returns the
+    counts (the intersection with each perturbation and with their union)
+    and the worst FP32-only cells."""
+    a = res[base]
+    e32 = np.abs(res[fp32]["peak"] - a["peak"]) > tol
+    pert = [k for k in res if k not in (base, fp32)]
+    sens = np.zeros_like(e32)
+    out = {"cells_fp32_over_tol": int(e32.sum()), "perturbations": {}}
+    for k in pert:
+        ek = np.abs(res[k]["peak"] - a["peak"]) > tol
+        sens |= ek
+        out["perturbations"][k] = {"cells_over_tol": int(ek.sum()), "fp32_cells_also_here": int((e32 & ek).sum())}
+    only = e32 & ~sens
+    out["cells_sensitive_union"] = int(sens.sum())
+    out["cells_fp32_only"] = int(only.sum())
+    d = np.abs(res[fp32]["peak"] - a["peak"])
+    idx = np.argsort(np.where(only, d, -1.0).ravel())[::-1][:min(8, int(only.sum()))]
+    out["worst_fp32_only"] = [{"row": int(i // d.shape[1]), "col": int(i % d.shape[1]), "err_m": float(d.flat[i]),
+                               "peak_fp64_m": float(a["peak"].flat[i])} for i in idx]
+    return out
+
+
+def run_precision_leg(args):
+    """Errors of the FP32 precision form against the FP64 path (itself
+    bit-identical to the oracle) on the 8192 x 8192 generator at a raster the
+    FP64 path finishes in minutes, over the generator's 3 h storm: peak depth
+    per cell, outlet peak discharge and its time, flood arrival time per cell
+    and the volume balance.  The FP64 run is repeated with its input
+    perturbed (rain scaled by 1 +- 1e-6, bed elevations moved by up to
+    1e-7 m, about the binary32 rounding of the FP32 form's bed offsets); a
+    cell whose FP32 peak error exceeds 1 mm while no perturbed run moves it
+    by 1 mm is counted as an FP32-only error."""
+    from sw2d_efdc_gb300 import api
+    members = [("fp64", api.FP64, 1.0, 0.0), ("fp32", api.FP32, 1.0, 0.0),
+               ("fp64_rain_plus_1e-6", api.FP64, 1.0 + 1e-6, 0.0)]
+    if args.prec_ensemble:
+        members += [("fp64_rain_minus_1e-6", api.FP64, 1.0 - 1e-6, 0.0), ("fp64_bed_1e-7", api.FP64, 1.0, 1e-7)]
+    size, T, dts = args.prec_size, args.prec_t, args.prec_sample
+    sc, res = precision_runs(size, T, dts, members, dev=device())
     a = res["fp64"]
-    return {
-        "workload": "precision form vs FP64 path: %dx%d, generator of the 8192x8192 case (dx 1 m, 1%% plane + "
-                    "bumps, gamma 5-min hyetograph mean 20 mm/h), %.0f s simulated, sampled every %.0f s"
-                    % (size, size, T, dts),
-        "fp32_vs_fp64": errors(a, res["fp32"]),
-        "fp64_vs_fp64_rain_1e-6": errors(a, res["fp64_perturbed"]),
-        "peak_depth_tolerance_m": 1e-3, "outlet_peak_q_fp64": float(np.max(a["q"])),
+    out = {
+        "workload": "precision form vs FP64 path: %dx%d of the 8192x8192 generator (dx 1 m, 1%% plane + bumps "
+                    "sigma 0.3 m corr 50 m, n 0.03, dry bed, gamma 5-min hyetograph shape 0.8 mean 20 mm/h, free "
+                    "south outlet, CFL 0.7), %.0f s simulated, sampled every %.0f s" % (size, size, T, dts),
+        "fp32_vs_fp64": precision_errors(a, res["fp32"]),
+        "peak_depth_tolerance_m": PREC_TOL_M, "outlet_peak_q_fp64": float(np.max(a["q"])),
         "arrival_cells": int(np.isfinite(a["arrival"]).sum()), "arrival_resolution_s": dts,
         "volume_balance_fp64": a["ledger"]["balance_error"], "volume_balance_fp32": res["fp32"]["ledger"]["balance_error"],
         "iterations_fp64": a["iters"], "iterations_fp32": res["fp32"]["iters"],
+        "wall_s": {k: round(v["wall_s"], 1) for k, v in res.items()},
+        "fp32_only": fp32_only_cells(res),
     }
+    for k in res:
+        if k.startswith("fp64_"):
+            out[k.replace("fp64_", "fp64_vs_fp64_")] = precision_errors(a, res[k])
+    return out
 
 
 def make_batch_specs(n, lo, hi, seed, t_scale=1.0):
@@ -380,7 +483,7 @@ def run_batched_leg(args, peak, fp64_value):
     for sp in specs:
         b.submit(**sp)
     b.step(0)
-    b.step(max(args.warmup, 3))
+    b.step(args.warmup)
     st0 = b.stats()
     with TimedRegion(args.profile_timed):
         b.step(args.steps)
@@ -468,9 +571,7 @@ def run_ours(args):
         dist.init_process_group("gloo")
     sc = workload_config2(args.size)
     cells = sc.rows * sc.cols
-    K = args.steps + (args.steps & 1)
-    W = max(args.warmup, 3)
-    W += W & 1
+    K, W = args.steps, args.warmup
 
     m = make_model(sc)
     load_inputs(m, sc)
@@ -597,6 +698,8 @@ def run_ours(args):
     if not args.no_fp32:
         out["fp32_precision_form"] = run_fp32_leg(args, peak)
         out["fp32_precision_form"]["vs_fp64_plain"] = round(out["fp32_precision_form"]["value"] / value, 3)
+    if not args.no_config1:
+        out["config1"] = run_config1_leg(args)
     if not args.no_prec:
         out["precision"] = run_precision_leg(args)
     if args.batch_n > 0:
@@ -620,22 +723,21 @@ def run_reference(args):
         return
     sc = workload_config2(args.size)
     threads = os.cpu_count() or 1
-    K = max(1, min(args.steps, args.cpu_iters))
+    K, W = args.steps, args.warmup
     # spin up into the wet regime with the reference's own GPU kernels, then
-    # time both of its builds from that depth
+    # time both of its builds from that depth: W untimed iterations, then K
     h_spun = reference_gpu_spinup(sc, args.spinup_s) if args.spinup_s > 0 else None
-    v, secs, n, kind, what = cpu_baseline_sample(sc, K, max(1, min(args.warmup, 2)), threads, h0=h_spun)
+    v, secs, n, kind, what = cpu_baseline_sample(sc, K, W, threads, h0=h_spun)
     ref_gpu = None
     if h_spun is not None:
-        Kg = max(args.steps, 10)
-        vg, secs_g, ng = cpu_reference_sample(sc, Kg, max(args.warmup, 3), 1, h0=h_spun, gpu=True)
+        vg, secs_g, ng = cpu_reference_sample(sc, K, W, 1, h0=h_spun, gpu=True)
         ref_gpu = {"value": round(vg, 5), "unit": UNIT, "ms_per_step": round(secs_g / ng * 1e3, 3), "steps": ng,
                    "kind": "reference kernels compiled by nvcc for sm_103a, the reference's launch "
                            "configuration (1024 threads, a device sync after each of the nine launches, "
                            "ql and rr copied to the device twice per iteration), wall clock"}
     out = {
         "metric": METRIC, "value": round(v, 5), "unit": UNIT, "n_gpus": world, "steps": n,
-        "warmup": max(1, min(args.warmup, 2)), "ms_per_step": round(secs / n * 1e3, 3),
+        "warmup": W, "ms_per_step": round(secs / n * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded spectral fractal DEM, Voronoi n, lognormal rain)",
         "config": {"workload": "plain SW2D FP64 %dx%d dx=2m pond-break" % (sc.rows, sc.cols),
@@ -652,12 +754,54 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_reference_gpu(args):
+    """The reference's own CUDA kernels on this GPU (nvcc sm_103a build, its
+    launch configuration and host loop), FIXED dt and uniform n, from the
+    depth after the same wet spin-up: the reference's GPU path as a line of
+    its own."""
+    rank, local, world = dist_env()
+    if rank != 0:
+        return
+    sc = workload_config2(args.size)
+    K, W = args.steps, args.warmup
+    h_spun = reference_gpu_spinup(sc, args.spinup_s) if args.spinup_s > 0 else None
+    from oracle import oracle as O
+    if O.ref_gpu_lib() is None:
+        print(json.dumps({"impl": "reference_gpu", "unavailable": "the reference's GPU build (oracle/_ref) is absent"}))
+        return
+    vg, secs, n = cpu_reference_sample(sc, K, W, 1, h0=h_spun if h_spun is not None else None, gpu=True)
+    print(json.dumps({
+        "metric": METRIC, "value": round(vg, 5), "unit": UNIT, "n_gpus": 1, "steps": n, "warmup": W,
+        "ms_per_step": round(secs / n * 1e3, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded spectral fractal DEM, Voronoi n, lognormal rain)",
+        "config": {"workload": "plain SW2D FP64 %dx%d dx=2m pond-break, FIXED dt 0.05 s, uniform n (the mean of "
+                               "the class table)" % (sc.rows, sc.cols), "cells": sc.rows * sc.cols},
+        "impl": "reference_gpu",
+        "kind": "reference kernels compiled by nvcc for sm_103a, the reference's launch configuration (1024 "
+                "threads, a device sync after each of the nine launches, ql and rr copied to the device twice per "
+                "iteration), wall clock",
+        "e2e": {"value": round(vg, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def launch_local_ranks(n: int) -> int:
+    """--gpus N without a launcher: start N local ranks (rank i on GPU i) with
+    torch.distributed.run on 127.0.0.1 and pass their output through; rank 0
+    prints the line."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=%d" % n,
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.run(cmd).returncode
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=4)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "reference_gpu"])
     ap.add_argument("--cpu-iters", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -671,8 +815,12 @@ def main():
     ap.add_argument("--profile-timed", action="store_true",
                     help="bracket the timed regions with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--no-prec", action="store_true", help="skip the precision-form error report")
+    ap.add_argument("--no-config1", action="store_true", help="skip the 256x256 whole-run line")
     ap.add_argument("--prec-size", type=int, default=2048)
-    ap.add_argument("--prec-t", type=float, default=3600.0)
+    ap.add_argument("--prec-t", type=float, default=3 * 3600.0,
+                    help="simulated seconds of the precision report (the generator's 3 h storm)")
+    ap.add_argument("--prec-ensemble", action="store_true",
+                    help="two more perturbed FP64 runs (rain x (1 - 1e-6), bed +- 1e-7 m) in the precision report")
     ap.add_argument("--prec-sample", type=float, default=20.0)
     ap.add_argument("--batch-n", type=int, default=256, help="scenarios of the batched leg (0 = skip)")
     ap.add_argument("--serve-n", type=int, default=48, help="requests of the served leg (0 = skip)")
@@ -683,8 +831,12 @@ def main():
                     help="simulated seconds before timing (600 s: the wet regime the 2 h run spends its time in)")
     ap.add_argument("--spinup-iters", type=int, default=0, help="iterations before timing (overrides --spinup-s)")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_local_ranks(args.gpus))
     if args.impl == "reference":
         run_reference(args)
+    elif args.impl == "reference_gpu":
+        run_reference_gpu(args)
     else:
         run_ours(args)
 

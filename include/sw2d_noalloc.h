@@ -29,12 +29,18 @@
  *    same time (from two host threads, on any streams) race and corrupt each
  *    other's results.  Serialise them.  A call returns only after `stream`
  *    has finished its work, so calls from one host thread never overlap.
- *  - The first call on each device does set-up: it looks up the scratch
- *    address with cudaGetSymbolAddress, with that device current, which may
- *    load the library's device code.  Make that first call before any stream
- *    capture begins on the device.
+ *  - The scratch address is per CUDA context: every call looks it up with
+ *    cudaGetSymbolAddress in the calling thread's current context (the
+ *    caller's current device), so a call after cudaDeviceReset, or under
+ *    another context of the same device, uses that context's own copy.  The
+ *    first call in a context may load the library's device code into it
+ *    (the set-up); make that first call before any stream capture begins on
+ *    the device.  Later lookups only read the address.
+ *  - Every call copies its two results to the host and synchronizes `stream`
+ *    before it returns.
  *  - The device used is the caller's current device; every array must live
- *    on it.
+ *    on it.  Rasters above 2^30 cells are rejected like the other entry
+ *    points' (SW2D_ERR_INVALID).
  */
 #ifndef SW2D_NOALLOC_H
 #define SW2D_NOALLOC_H

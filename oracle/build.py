@@ -29,7 +29,10 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
-REFERENCE_ROOT = os.environ.get("SW2D_REFERENCE_ROOT", "/root/reference")
+# The reference checkout: $SW2D_REFERENCE_ROOT, else a checkout named
+# "reference" beside this repository (../reference from the repo root).
+REFERENCE_ROOT = os.environ.get("SW2D_REFERENCE_ROOT",
+                                os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 REFERENCE_CU = os.path.join(REFERENCE_ROOT, "SW2D-EFDC.cu")
 
 ORACLE_LIB = os.path.join(BUILD_DIR, "libsw2d_oracle.so")

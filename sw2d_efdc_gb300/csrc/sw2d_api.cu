@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <memory>
 #include <thread>
@@ -535,9 +536,23 @@ int run_until(sw2d_handle* h, double t_end, long long max_iters, int64_t* done_o
         if ((rc = launch_iterations(h, ne))) return rc;
         launched = ne;
     } else if (max_iters >= 0) {
-        /* a bounded CFL run launches exactly max_iters (even) iterations */
-        if ((rc = launch_iterations(h, max_iters))) return rc;
-        launched = max_iters;
+        /* a bounded CFL run: an odd count launches one iteration more, which
+         * the device's iteration limit leaves inactive (a state copy), so the
+         * state ends in buffer 0 as the captured pairs need */
+        const long long ne = max_iters + (max_iters & 1);
+        if (max_iters & 1) {
+            const long long lim = it0 + max_iters;
+            if ((rc = put(h, &h->clk->iter_end, &lim, sizeof lim))) return rc;
+            if ((rc = prime(h, 0))) return rc;
+        }
+        rc = launch_iterations(h, ne);
+        if (max_iters & 1) {
+            const long long none = LLONG_MAX;
+            const int rc2 = put(h, &h->clk->iter_end, &none, sizeof none);
+            if (!rc) rc = rc2;
+        }
+        if (rc) return rc;
+        launched = ne;
     } else {
         for (;;) {
             if ((rc = launch_iterations(h, kChunk))) return rc;
@@ -692,6 +707,7 @@ int sw2d_create(const sw2d_config* cfg, sw2d_handle** out) {
     for (int k = 0; k < 8; k++) cudaEventCreate(&h->kev[k]);
     h->kernel_ms.assign(8, 0.0);
     DevClock c{};
+    c.iter_end = LLONG_MAX;
     c.t = cfg->t0;
     c.t_end = cfg->t0;
     if (cudaMemcpy(h->clk, &c, sizeof c, cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -803,6 +819,7 @@ int sw2d_set_depth(sw2d_handle* h, const double* d) {
     if ((rc = zero(h, h->drys, h->ncell))) return rc;
     if ((rc = upload_interior(h, h->h[0], dd.data(), h->R, h->C))) return rc;
     DevClock c{};
+    c.iter_end = LLONG_MAX;
     c.t = h->cfg.t0;
     c.t_end = h->cfg.t0;
     if ((rc = put(h, h->clk, &c, sizeof c))) return rc;
@@ -993,9 +1010,6 @@ int sw2d_step(sw2d_handle* h, int n, double t_end) {
     sw2d::NvtxRange r("sw2d_step");
     if (n < 0) return fail(SW2D_ERR_INVALID, "n < 0");
     int64_t done = 0;
-    if (h && !h->fp32() && h->cfg.dt_mode == SW2D_DT_CFL && (n & 1)) {
-        return fail(SW2D_ERR_INVALID, "CFL mode steps in pairs of iterations");
-    }
     return run_until(h, t_end, n, &done);
 }
 

@@ -3,7 +3,7 @@
  *
  * A work item is a 224-column strip x `seg` rows of one scenario, taken by a
  * CTA of four warps.  Thread 0 streams the strip's rows (232 columns with a
- * 4-cell halo) of depth, bed offset and x/y discharges into a three-block
+ * 4-cell halo) of depth, bed offset and x/y discharges into a two-block
  * ring in shared memory with 2-D TMA loads (cp.async.bulk.tensor, one
  * mbarrier per block, four rows per block).  Each warp owns 64 staged
  * columns, two per lane, of which 56 are its output; it marches down the
@@ -412,7 +412,22 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 }
             }
             if (__syncthreads_or(!ok)) {
-                if (tid == 0) atomicOr(&clk->status, 2);
+                if (tid == 0) {
+                    atomicOr(&clk->status, 2);
+                    /* Blocks b .. b+NS-1 were issued (none under the staging
+                     * stall of the failure test) and their loads may still
+                     * be in flight into this CTA's shared memory: wait for
+                     * them, again bounded, before the CTA exits and its
+                     * shared memory is handed to another CTA.  The launch's
+                     * results are void either way (status bit 1). */
+                    const int issued = P.stall_staging ? 0 : min(nblk, b + NS);
+                    for (int bb = b; bb < issued; bb++) {
+                        const long long t1 = clock64();
+                        while (!mbar_try_wait(&S.bar[bb % NS], (unsigned)((bb / NS) & 1)) &&
+                               clock64() - t1 <= (1ll << 31)) {
+                        }
+                    }
+                }
                 return;
             }
         }

@@ -550,7 +550,9 @@ __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
                 p.outlet[2 * k + 1] = clk->led[LED_QOUT];
                 clk->outlet_n += 1;
             }
-            prepare_slot(p, &clk->slot[cur ^ 1], clk->t, clk->s_max, clk->t_end);
+            /* past the iteration limit the next slot is inactive: t_end = t */
+            prepare_slot(p, &clk->slot[cur ^ 1], clk->t, clk->s_max,
+                         clk->iters < clk->iter_end ? clk->t_end : clk->t);
         } else {
             clk->slot[cur ^ 1] = s;
         }
@@ -689,7 +691,8 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int
             clk->led[LED_SMAX] = clk->s_max;
             clk->led[LED_VOLUME0] = clk->led[LED_VOLUME];
         }
-        if (full != 1) prepare_slot(p, &clk->slot[cur], clk->t, clk->s_max, clk->t_end);
+        if (full != 1)
+            prepare_slot(p, &clk->slot[cur], clk->t, clk->s_max, clk->iters < clk->iter_end ? clk->t_end : clk->t);
         clk->counter = 0;
     }
 }

@@ -62,6 +62,7 @@ struct DevClock {
     unsigned int counter; /* last-block ticket of the reduction kernels */
     int status;           /* bit 0: non-finite volume seen */
     long long outlet_n;
+    long long iter_end;   /* the slot after iteration iter_end is inactive (a state copy) */
 };
 
 /* Everything a step kernel needs, passed by value. */

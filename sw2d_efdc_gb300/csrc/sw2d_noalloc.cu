@@ -15,7 +15,6 @@
 
 #include <cmath>
 #include <cstdio>
-#include <mutex>
 
 namespace sw2d {
 void set_error_message(const char* msg); /* sw2d_api.cu: the message sw2d_last_error returns */
@@ -30,7 +29,6 @@ constexpr int kSlots = 3;                             /* volume, x speed bits, y
 constexpr int kResult = kSlots * kMaxTiles;           /* volume * area, speed */
 constexpr int kCounter = kResult + 2;                 /* tile-completion counter (low 32 bits) */
 constexpr int kScratchDoubles = kCounter + 1;         /* 49,155 doubles = 393,240 bytes */
-constexpr int kMaxDevices = 64;
 
 /* The scratch: kSlots partials per tile, the two results, the counter. */
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
@@ -160,9 +158,6 @@ __global__ void __launch_bounds__(256) k64_measure_noalloc(const double* __restr
     }
 }
 
-std::mutex g_addr_mu;
-double* g_addr[kMaxDevices] = {};
-
 int reject(int code, const char* msg) {
     sw2d::set_error_message(msg);
     return code;
@@ -186,7 +181,10 @@ extern "C" int sw2d_measure_state_noalloc(const double* d_dem, const double* d_d
     if (rows < 1 || cols < 1) return reject(SW2D_ERR_INVALID, "rows and cols must be >= 1");
     if (!(dx > 0.0) || !(dy > 0.0) || !(th > 0.0) || !(g > 0.0))
         return reject(SW2D_ERR_INVALID, "dx, dy, th and g must be > 0");
-    const long long tiles_x = (cols + kTile - 1) / kTile, tiles_y = (rows + kTile - 1) / kTile;
+    if (static_cast<long long>(rows) * cols > (1LL << 30))
+        return reject(SW2D_ERR_INVALID, "rows * cols above 2^30 cells");
+    const long long tiles_x = (static_cast<long long>(cols) + kTile - 1) / kTile;
+    const long long tiles_y = (static_cast<long long>(rows) + kTile - 1) / kTile;
     if (tiles_x * tiles_y > kMaxTiles) {
         char buf[200];
         std::snprintf(buf, sizeof buf,
@@ -195,22 +193,16 @@ extern "C" int sw2d_measure_state_noalloc(const double* d_dem, const double* d_d
                       rows, cols, tiles_x * tiles_y, kMaxTiles);
         return reject(SW2D_ERR_INVALID, buf);
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail("cudaGetDevice", e);
-    if (dev < 0 || dev >= kMaxDevices) return reject(SW2D_ERR_INVALID, "device index beyond 63");
-    double* scratch = nullptr;
-    {
-        /* set-up, once per device, with that device current */
-        std::lock_guard<std::mutex> lock(g_addr_mu);
-        if (!g_addr[dev]) {
-            void* p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess) return cuda_fail("cudaGetSymbolAddress", e);
-            g_addr[dev] = static_cast<double*>(p);
-        }
-        scratch = g_addr[dev];
-    }
+    /* The scratch array's device address belongs to the calling thread's
+     * current context (one copy per device, and a fresh copy after
+     * cudaDeviceReset or under another context), so it is looked up on every
+     * call rather than cached.  The lookup allocates nothing; in a context
+     * that has not used the library's device code yet it loads that code
+     * first, which is this entry point's one-time set-up. */
+    void* addr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail("cudaGetSymbolAddress", e);
+    double* scratch = static_cast<double*>(addr);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     /* the counter must be zero when the kernel starts */
     e = cudaMemsetAsync(scratch + kCounter, 0, sizeof(double), s);

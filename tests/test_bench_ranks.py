@@ -66,7 +66,7 @@ def test_reference_arm_line_on_the_cpu():
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     env = {k: v for k, v in os.environ.items() if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE")}
     out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--size", "256", "--steps", "3",
-                          "--warmup", "3", "--spinup-s", "0"], cwd=root, env=env, capture_output=True, text=True,
+                          "--warmup", "5", "--spinup-s", "0"], cwd=root, env=env, capture_output=True, text=True,
                          timeout=300)
     assert out.returncode == 0, out.stderr[-2000:]
     line = json.loads(out.stdout.strip().splitlines()[-1])
@@ -75,6 +75,29 @@ def test_reference_arm_line_on_the_cpu():
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["cells"] == 256 * 256
+    assert line["steps"] == 3 and line["warmup"] == 5  # both counts honoured exactly
+
+
+def test_gpus_flag_spawns_local_ranks_and_prints_one_line():
+    # --gpus 2 without a launcher starts two local ranks; rank 0 alone runs
+    # the reference arm and prints the one line, the other rank exits 0
+    import json
+    import subprocess
+    import sys
+    from oracle import oracle as O
+    if O.ref_lib() is None:
+        pytest.skip("reference CPU build unavailable")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "LOCAL_RANK", "WORLD_SIZE", "MASTER_PORT")}
+    out = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--size", "128",
+                          "--steps", "3", "--warmup", "5", "--spinup-s", "0"], cwd=root, env=env,
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["n_gpus"] == 2 and line["impl"] == "reference"
+    assert line["steps"] == 3 and line["warmup"] == 5
 
 
 def test_cpu_baseline_falls_back_to_the_port(monkeypatch):

@@ -150,6 +150,23 @@ def test_step_counts_and_odd_steps():
     _assert_same(_fields(m), od.fields())
 
 
+def test_cfl_odd_step_counts():
+    """CFL mode takes any iteration count: an odd bounded count ends with an
+    inactive iteration the device's iteration limit sets up."""
+    case = bumpy_case(t_end=1e9, dt_mode=O.DT_CFL, cfl=0.7, dt_max=1.0, outflow_south=True)
+    m = model_from_case(case)
+    od = O.Oracle(case, math=O.MATH_DEVICE)
+    for n in (1, 3, 2, 7, 5):
+        m.step(n)
+        od.run(max_iters=n)
+        assert m.time() == (od.time, od.iters)
+    assert od.iters == 18
+    _assert_same(_fields(m), od.fields())
+    lg, lo = m.ledger(), od.ledger()
+    assert lg["s_max"] == lo["s_max"] and lg["dt_last"] == lo["dt2_last"]
+    m.close()
+
+
 def test_snapshot_restore_is_exact():
     case = bumpy_case(t_end=1e9)
     m = model_from_case(case)

@@ -70,6 +70,24 @@ def test_noalloc_measure_matches_the_fp64_handle():
     m.close()
 
 
+@pytest.mark.parametrize("rows,cols", [(600, 700), (4096, 4096)])
+def test_noalloc_measure_many_tiles(rows, cols):
+    """More tiles than the combining block has threads (600 x 700 = 418
+    tiles: the strided combine), and the largest raster the scratch holds
+    (4096 x 4096 = 16,384 tiles)."""
+    rng = np.random.default_rng(rows + cols)
+    dem = 0.01 * (rows - np.arange(rows))[:, None] + 0.2 * rng.standard_normal((rows, cols))
+    dem[rows // 3: rows // 3 + 5, cols // 2: cols // 2 + 9] = -9999.0
+    h0 = np.where(rng.random((rows, cols)) < 0.5, 0.3 * rng.random((rows, cols)), 0.0)
+    h0[dem == -9999.0] = 0.0
+    case = O.Case(dem=dem, h0=h0, cellsize=2.0, manning=0.03, dt_mode=O.DT_CFL, cfl=0.7, dt_max=0.5,
+                  rain=np.array([20.0, 20.0, 20.0]), dtrain=3600.0, t_end=1e9)
+    m = model_from_case(case)
+    m.step(4)
+    _check_state(m, case, _device(case.dem))
+    m.close()
+
+
 def test_noalloc_measure_rejects_rasters_beyond_its_scratch():
     lib = api.load()
     d = torch.zeros(1, dtype=torch.float64, device="cuda")
@@ -79,3 +97,8 @@ def test_noalloc_measure_rejects_rasters_beyond_its_scratch():
                                         api.C.byref(vol), api.C.byref(spd))
     assert rc == -1
     assert b"16384" in lib.sw2d_last_error()
+    # sizes whose tile counts would overflow int arithmetic are refused too
+    for r, c in ((2147483647, 2147483647), (1 << 16, 1 << 15)):
+        rc = lib.sw2d_measure_state_noalloc(p, p, p, p, r, c, 1.0, 1.0, -9999.0, 1e-4, 9.8, None,
+                                            api.C.byref(vol), api.C.byref(spd))
+        assert rc == -1
