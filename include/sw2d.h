@@ -222,6 +222,15 @@ int sw2d_write_efdc_cards(const char* path, int n_faces, const int* side, const 
  * reference's sweep order (last raster row first, each row west to east,
  * updated values feeding later cells).  Host only. */
 int sw2d_lake_catchment_smooth(int rows, int cols, const int* mask, double* dem);
+/* The same DEM pre-pass on the device, in place on caller-owned device
+ * arrays (d_mask: rows*cols ints, d_dem: rows*cols doubles, reference
+ * orientation), on `stream` (NULL = the legacy default stream): the lake-edge
+ * cells listed per anti-diagonal, then a wavefront over the diagonals, which
+ * keeps the reference's sweep order (a cell reads its south and west
+ * neighbours after their update), bit-identical to sw2d_lake_catchment_smooth.
+ * Allocates a scratch list of the edge cells; synchronizes `stream` before
+ * it returns.  Replaces the host loop of SW2D-EFDC.cu:2766-2827. */
+int sw2d_lake_catchment_smooth_device(int rows, int cols, const int* d_mask, double* d_dem, void* stream);
 /* Evaporation series for sw2d_set_evaporation_series: n values in mm per
  * dtrain from air temperature (deg C) and global radiation (W/m2), by the
  * energy-balance method of gpu_evaporation_calc (SW2D-EFDC.cu:556-586),

@@ -133,6 +133,7 @@ SIGNATURES = {
     "sw2d_write_qser": (C.c_int, [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_int, _ip, C.c_int, _dp, _dp]),
     "sw2d_write_efdc_cards": (C.c_int, [C.c_char_p, C.c_int, _ip, _ip, _ip, C.c_int, C.c_int, C.c_int]),
     "sw2d_lake_catchment_smooth": (C.c_int, [C.c_int, C.c_int, _ip, _dp]),
+    "sw2d_lake_catchment_smooth_device": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sw2d_test_stall_staging": (C.c_int, [C.c_void_p, C.c_int]),
     "sw2d_evaporation_series": (C.c_int, [C.c_int, _dp, _dp, C.c_double, C.c_double, _dp]),
     "sw2d_manning_classes_of": (C.c_int, [C.c_int64, _dp, C.c_int, _u8p, _dp, C.POINTER(C.c_int)]),
@@ -535,6 +536,14 @@ def lake_catchment_smooth(mask, dem):
     _check(load().sw2d_lake_catchment_smooth(z.shape[0], z.shape[1], _ptr(m, _ip), _ptr(z, _dp)),
            "sw2d_lake_catchment_smooth")
     return z
+
+
+def lake_catchment_smooth_device(rows, cols, d_mask, d_dem, stream=None):
+    """The DEM pre-pass on device arrays (pointers to rows*cols int32 mask
+    and float64 DEM on the current device), in place."""
+    _check(load().sw2d_lake_catchment_smooth_device(int(rows), int(cols), C.c_void_p(d_mask), C.c_void_p(d_dem),
+                                                    C.c_void_p(stream) if stream else None),
+           "sw2d_lake_catchment_smooth_device")
 
 
 def evaporation_series(temp, rad, albedo, dtrain):

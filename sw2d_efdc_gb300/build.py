@@ -35,6 +35,7 @@ UNITS = {
     "sw2d_noalloc.cu": ["--fmad=false", "-Xptxas", "-v"],
     "sw2d_efdc_io.cu": [],
     "sw2d_case_prep.cu": ["-Xcompiler", "-ffp-contract=off"],
+    "sw2d_lake_dev.cu": ["--fmad=false"],
 }
 HEADERS = ["sw2d_internal.h", "sw2d_math.h", "sw2d_fp32.h", "sw2d_engine.h"]
 
@@ -88,13 +89,16 @@ def build(verbose: bool = False) -> str:
 
 def build_cli() -> str:
     """The case driver (csrc/sw2d_cli.cpp): host C++ linked against
-    libsw2d.so beside it (rpath $ORIGIN)."""
+    libsw2d.so beside it (rpath $ORIGIN) and the CUDA runtime (the device
+    copies of the lake-edge pre-pass)."""
     src = os.path.join(CSRC, "sw2d_cli.cpp")
     deps = [src, LIB, os.path.join(ROOT, "include", "sw2d.h"), __file__]
     if _stale(CLI, deps):
         cxx = shutil.which("g++") or "g++"
-        cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include"), src,
-               "-o", CLI + ".tmp", "-L", OUT_DIR, "-lsw2d", "-Wl,-rpath,$ORIGIN", "-pthread"]
+        cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+        cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-I", os.path.join(ROOT, "include"),
+               "-I", os.path.join(cuda, "include"), src, "-o", CLI + ".tmp", "-L", OUT_DIR, "-lsw2d",
+               "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN", "-pthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("sw2d_cli build failed:\n%s\n%s" % (r.stdout, r.stderr))

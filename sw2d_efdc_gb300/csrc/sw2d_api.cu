@@ -66,7 +66,6 @@ struct sw2d_handle {
     double* qy[2] = {nullptr, nullptr};
     double* uu1 = nullptr;
     double* vv1 = nullptr;
-    uint8_t* drys = nullptr;
     uint8_t* mcls = nullptr;
     double* mtab = nullptr;
     double* gnn = nullptr; /* friction coefficient per class pair */
@@ -180,7 +179,6 @@ struct sw2d_handle {
         }
         p.uu1 = uu1;
         p.vv1 = vv1;
-        p.drys = drys;
         p.partials = partials;
         p.partials_f = partials_f;
         p.outlet = outlet;
@@ -693,7 +691,6 @@ int sw2d_create(const sw2d_config* cfg, sw2d_handle** out) {
     }
     TRY(dalloc(&h->uu1, h->ncell));
     TRY(dalloc(&h->vv1, h->ncell));
-    TRY(dalloc(&h->drys, h->ncell));
     TRY(dalloc(&h->partials, (size_t)h->params().nblocks_cells * 4 + 8));
     TRY(dalloc(&h->partials_f, (size_t)h->params().nblocks_faces * 2 + 8));
     TRY(dalloc(&h->clk, 1));
@@ -740,7 +737,6 @@ int sw2d_destroy(sw2d_handle* h) {
     }
     dfree(h->uu1);
     dfree(h->vv1);
-    dfree(h->drys);
     dfree(h->mcls);
     dfree(h->mtab);
     dfree(h->gnn);
@@ -816,7 +812,6 @@ int sw2d_set_depth(sw2d_handle* h, const double* d) {
     }
     if ((rc = zero(h, h->uu1, h->ncell * sizeof(double)))) return rc;
     if ((rc = zero(h, h->vv1, h->ncell * sizeof(double)))) return rc;
-    if ((rc = zero(h, h->drys, h->ncell))) return rc;
     if ((rc = upload_interior(h, h->h[0], dd.data(), h->R, h->C))) return rc;
     DevClock c{};
     c.iter_end = LLONG_MAX;
@@ -1319,7 +1314,6 @@ int sw2d_restore(sw2d_handle* h, const void* buf, size_t bytes) {
         if ((rc = put(h, dst[k], p, h->ncell * sizeof(double)))) return rc;
         p += h->ncell * sizeof(double);
     }
-    if ((rc = zero(h, h->drys, h->ncell))) return rc;
     h->have_depth = true;
     StepParams sp = h->params();
     fp64_launch_face_velocity(sp, 0, h->stream);

@@ -33,6 +33,8 @@
  */
 #include "sw2d.h"
 
+#include <cuda_runtime.h>
+
 #include <sys/stat.h>
 #include <sys/types.h>
 
@@ -612,6 +614,30 @@ void print_check(const Case& c, const std::vector<Event>& ev, long long iters) {
     std::printf("}\n");
 }
 
+
+/* The coupled run's DEM pre-pass (lake_catchment_smooth, SW2D-EFDC.cu:2766-2827)
+ * on the device: the mask and the DEM are copied to the run's GPU, smoothed
+ * there by the library's wavefront pass and copied back before the DEM is
+ * loaded. */
+static void smooth_lake_edges_on_device(int device, int R, int C, const std::vector<int>& mask,
+                                        std::vector<double>& dem) {
+    const size_t n = (size_t)R * C;
+    int* dm = nullptr;
+    double* dz = nullptr;
+    bool ok = cudaSetDevice(device) == cudaSuccess && cudaMalloc(&dm, n * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&dz, n * sizeof(double)) == cudaSuccess &&
+              cudaMemcpy(dm, mask.data(), n * sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(dz, dem.data(), n * sizeof(double), cudaMemcpyHostToDevice) == cudaSuccess;
+    if (ok) check(sw2d_lake_catchment_smooth_device(R, C, dm, dz, nullptr), "sw2d_lake_catchment_smooth_device");
+    ok = ok && cudaMemcpy(dem.data(), dz, n * sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess;
+    cudaFree(dm);
+    cudaFree(dz);
+    if (!ok) {
+        std::fprintf(stderr, "sw2d_cli: CUDA error in the lake-edge pre-pass: %s\n", cudaGetErrorString(cudaGetLastError()));
+        std::exit(1);
+    }
+}
+
 void run_case(Case& c, const Options& o) {
     const Grid& g = c.grid;
     const int R = g.rows, C = g.cols;
@@ -634,7 +660,7 @@ void run_case(Case& c, const Options& o) {
         FILE* f = open_out(join(efdc_dir, "EFDC.INP"));
         std::fwrite(tpl.data(), 1, tpl.size(), f);
         std::fclose(f);
-        check(sw2d_lake_catchment_smooth(R, C, c.mask.data(), c.dem.data()), "sw2d_lake_catchment_smooth");
+        smooth_lake_edges_on_device(o.device, R, C, c.mask, c.dem);
     }
     FILE* wl = open_out(join(out_dir, "WaterLevel.txt"));
     if (c.out_outlet != 1) std::fprintf(wl, "%s\n", "Outlet off");

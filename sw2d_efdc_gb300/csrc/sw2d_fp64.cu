@@ -3,20 +3,20 @@
  *
  * GB300's FP64 pipe runs at ~1/64 of the FP32 rate, so this path is bound by
  * FP64 instructions, not HBM.  The step is therefore split so that nothing
- * FP64 is computed twice:
+ * FP64 is computed twice, in two kernels per iteration:
  *   k64_flux   : new x/y face discharges of every face (flux, :97-353) from the
- *                stored face velocities uu1/vv1 of the previous iteration
- *   k64_hstar  : provisional depth (continuity at t, :602-664) -> one byte
- *                per cell "active and h* < th" (the treat_error predicate)
- *   k64_depth  : closes outward faces of those cells on the fly (treat_error,
- *                :695-725, restated per face), final depth at t+dt, FP64
- *                volume / rain / clamp / outlet sums and the CFL speed
- *                maximum by block reduction; the last block reduces the
+ *                stored face velocities uu1/vv1 of the previous iteration,
+ *                and the CFL face-speed maxima of the entering state
+ *   k64_update : per tile, the provisional depth (continuity at t,
+ *                :602-664) -> "active and h* < th" flags in shared memory;
+ *                treat_error (:695-725, restated per face) and the final
+ *                depth at t+dt; the closed faces written back and the face
+ *                velocities uu1 = qx/hm, vv1 = qy/hn of the new state
+ *                (hm_hn, uu1_vv1, :362-452); FP64 volume / rain / clamp /
+ *                outlet sums by block reduction; the last block reduces the
  *                per-block partials in a fixed order and prepares the next
- *                iteration's length and forcing on the device
- *   k64_facevel: writes the closed faces back and the face velocities
- *                uu1 = qx/hm, vv1 = qy/hn of the new state (hm_hn, uu1_vv1,
- *                :362-452); forward (:670-693) is a buffer swap.
+ *                iteration's length and forcing on the device.
+ * forward (:670-693) is a buffer swap.
  * Compiled with --fmad=false: every expression is evaluated with the same
  * roundings as the CPU oracle (gcc -ffp-contract=off), explicit fma() only
  * where sw2d_math.h spells it.
@@ -404,23 +404,6 @@ __device__ __forceinline__ double continuity(const StepParams& p, size_t i, uint
     return hn;
 }
 
-__global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_hstar(StepParams p, int cur) {
-    const int c = blockIdx.x * SW2D_BX + threadIdx.x;
-    const int r = blockIdx.y * SW2D_BY + threadIdx.y;
-    if (r >= p.R || c >= p.C) return;
-    const Slot& s = p.clk->slot[cur];
-    if (!s.active) return;
-    const int nxt = cur ^ 1;
-    const size_t i = (size_t)(r + H) * p.P + (c + H);
-    const uint8_t f = p.flags[i];
-    const double* __restrict__ fx = p.qx[nxt];
-    const double* __restrict__ fy = p.qy[nxt];
-    double raw, rt;
-    const double hs = continuity(p, i, f, p.h[cur][i], fx[i + p.P] - fx[i], fy[i + 1] - fy[i], s.dt2,
-                                 s.rr1, s.ev1, s.ql1, &raw, &rt);
-    p.drys[i] = (uint8_t)((f & SW2D_F_ACTIVE) && sw2d_lt_pos(hs, p.th));
-}
-
 /* ------------------------------------------------------------------------ */
 /* block reductions (fixed order: deterministic for a given grid)            */
 
@@ -560,56 +543,141 @@ __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
     }
 }
 
-__global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_depth(StepParams p, int cur) {
+/* ------------------------------------------------------------------------ */
+/* continuity at t, treat_error, continuity at t+dt, hm_hn + uu1_vv1:         */
+/* SW2D-EFDC.cu:602-664, :695-725, :362-452 in one pass                       */
+
+/* Tile of the update kernel: UT_W x UT_H cells (and their north and west
+ * faces) per CTA.  The provisional depths ("dry" flags) are evaluated on the
+ * tile plus two rows north and west and one row south and east, the new
+ * depths on the tile plus the row north and the column west: the faces of
+ * the tile read both; the halo is recomputed, not exchanged. */
+#define UT_W 64
+#define UT_H 16
+#define UT_DW (UT_W + 3)
+#define UT_DH (UT_H + 3)
+#define UT_NW (UT_W + 1)
+#define UT_NH (UT_H + 1)
+
+__global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_update(StepParams p, int cur) {
+    __shared__ uint8_t sdry[UT_DH][UT_DW];   /* rows r0-2 .. r0+UT_H, cols c0-2 .. c0+UT_W */
+    __shared__ double shn[UT_NH][UT_NW];     /* rows r0-1 .. r0+UT_H-1, cols c0-1 .. c0+UT_W-1 */
     __shared__ double smd[NWARP];
-    const int c = blockIdx.x * SW2D_BX + threadIdx.x;
-    const int r = blockIdx.y * SW2D_BY + threadIdx.y;
+    const int tid = threadIdx.x;
+    const int c0 = blockIdx.x * UT_W, r0 = blockIdx.y * UT_H;
     const int nxt = cur ^ 1;
     const Slot& s = p.clk->slot[cur];
+    const int P = p.P, R = p.R, C = p.C;
+    const double th = p.th;
+    const double* __restrict__ fx = p.qx[nxt];
+    const double* __restrict__ fy = p.qy[nxt];
+    const double* __restrict__ hc = p.h[cur];
     double vr = 0.0, ve = 0.0, vq = 0.0;
-    double fN = 0, fS = 0, fW = 0, fE = 0, hn = 0;
-    if (r < p.R && c < p.C) {
-        const int P = p.P;
-        const size_t i = (size_t)(r + H) * P + (c + H);
-        if (!s.active) {
-            p.h[nxt][i] = p.h[cur][i];
-        } else {
-            const uint8_t f = p.flags[i];
-            const double* __restrict__ fx = p.qx[nxt];
-            const double* __restrict__ fy = p.qy[nxt];
-            const uint8_t* __restrict__ d = p.drys;
-            const uint8_t dc = d[i];
-            /* treat_error per face: a face carrying water out of a cell whose
-             * provisional depth fell below th is closed (:704-719) */
-            fN = fx[i];
-            fS = fx[i + P];
-            fW = fy[i];
-            fE = fy[i + 1];
-            if ((sw2d_gt0(fN) && d[i - P]) || (sw2d_lt0(fN) && dc)) fN = 0;
-            if ((sw2d_gt0(fS) && dc) || (sw2d_lt0(fS) && d[i + P])) fS = 0;
-            if ((sw2d_gt0(fW) && d[i - 1]) || (sw2d_lt0(fW) && dc)) fW = 0;
-            if ((sw2d_gt0(fE) && dc) || (sw2d_lt0(fE) && d[i + 1])) fE = 0;
-            const double ho = p.h[cur][i];
-            double raw, rt;
-            hn = continuity(p, i, f, ho, fS - fN, fE - fW, s.dt2, s.rr2, s.ev2, s.ql2, &raw, &rt);
-            p.h[nxt][i] = hn;
-            if (f & SW2D_F_ACTIVE) {
-                if (sw2d_lt0(raw)) atomicAdd(&p.clk->led[LED_CLAMP], -raw * p.area); /* max(h, 0) gain */
-                if (p.ledger_cells) {
-                    vr = rt;
-                    ve = sw2d_gt(ho, p.ev_wl_min) ? s.ev2 : 0.0;
+    if (!s.active) {
+        /* the loop condition failed: the iteration copies the depth */
+        for (int k = tid; k < UT_W * UT_H; k += SW2D_BX * SW2D_BY) {
+            const int r = r0 + k / UT_W, c = c0 + k % UT_W;
+            if (r < R && c < C) {
+                const size_t i = (size_t)(r + H) * P + (c + H);
+                p.h[nxt][i] = hc[i];
+            }
+        }
+    } else {
+        /* 1: provisional depth at t -> "active and h* < th" (0 outside the raster) */
+        for (int k = tid; k < UT_DH * UT_DW; k += SW2D_BX * SW2D_BY) {
+            const int rr = k / UT_DW, cc = k - rr * UT_DW;
+            const int r = r0 - 2 + rr, c = c0 - 2 + cc;
+            uint8_t dflag = 0;
+            if (r >= 0 && r < R && c >= 0 && c < C) {
+                const size_t i = (size_t)(r + H) * P + (c + H);
+                const uint8_t f = p.flags[i];
+                double raw, rt;
+                const double hs = continuity(p, i, f, hc[i], fx[i + P] - fx[i], fy[i + 1] - fy[i], s.dt2, s.rr1,
+                                             s.ev1, s.ql1, &raw, &rt);
+                dflag = (uint8_t)((f & SW2D_F_ACTIVE) && sw2d_lt_pos(hs, th));
+            }
+            sdry[rr][cc] = dflag;
+        }
+        __syncthreads();
+        /* 2: treat_error per face (a face carrying water out of a cell whose
+         * provisional depth fell below th is closed, :704-719), final depth
+         * at t+dt; written for the tile's own cells, kept in shared memory
+         * for the faces */
+        for (int k = tid; k < UT_NH * UT_NW; k += SW2D_BX * SW2D_BY) {
+            const int rr = k / UT_NW, cc = k - rr * UT_NW;
+            const int r = r0 - 1 + rr, c = c0 - 1 + cc;
+            double hn = 0.0;
+            if (r >= 0 && r < R && c >= 0 && c < C) {
+                const size_t i = (size_t)(r + H) * P + (c + H);
+                const uint8_t f = p.flags[i];
+                const int dr = rr + 1, dc = cc + 1;
+                const uint8_t dC = sdry[dr][dc];
+                double fN = fx[i], fS = fx[i + P], fW = fy[i], fE = fy[i + 1];
+                if ((sw2d_gt0(fN) && sdry[dr - 1][dc]) || (sw2d_lt0(fN) && dC)) fN = 0;
+                if ((sw2d_gt0(fS) && dC) || (sw2d_lt0(fS) && sdry[dr + 1][dc])) fS = 0;
+                if ((sw2d_gt0(fW) && sdry[dr][dc - 1]) || (sw2d_lt0(fW) && dC)) fW = 0;
+                if ((sw2d_gt0(fE) && dC) || (sw2d_lt0(fE) && sdry[dr][dc + 1])) fE = 0;
+                const double ho = hc[i];
+                double raw, rt;
+                hn = continuity(p, i, f, ho, fS - fN, fE - fW, s.dt2, s.rr2, s.ev2, s.ql2, &raw, &rt);
+                if (rr >= 1 && cc >= 1) { /* the tile's own cell */
+                    p.h[nxt][i] = hn;
+                    if (f & SW2D_F_ACTIVE) {
+                        if (sw2d_lt0(raw)) atomicAdd(&p.clk->led[LED_CLAMP], -raw * p.area); /* max(h, 0) gain */
+                        if (p.ledger_cells) {
+                            vr += rt;
+                            ve += sw2d_gt(ho, p.ev_wl_min) ? s.ev2 : 0.0;
+                        }
+                        if (r == R - 1) vq += fS;
+                    }
                 }
-                if (r == p.R - 1) vq = fS;
+            }
+            shn[rr][cc] = hn;
+        }
+        __syncthreads();
+        /* 3: the closed faces written back and the face velocities of the new
+         * state, uu1 = qx/hm and vv1 = qy/hn (hm_hn, uu1_vv1), for the
+         * tile's north and west faces (the raster's south and east edge
+         * faces in the last tile row / column) */
+        for (int k = tid; k < UT_H * UT_W; k += SW2D_BX * SW2D_BY) {
+            const int rr = k / UT_W, cc = k - rr * UT_W;
+            const int r = r0 + rr, c = c0 + cc;
+            if (r > R || c > C) continue;
+            const size_t i = (size_t)(r + H) * P + (c + H);
+            const int dr = rr + 2, dc = cc + 2, nr = rr + 1, nc = cc + 1;
+            if (c < C) {
+                double F = fx[i];
+                if ((sw2d_gt0(F) && sdry[dr - 1][dc]) || (sw2d_lt0(F) && sdry[dr][dc])) {
+                    F = 0;
+                    p.qx[nxt][i] = F;
+                }
+                double hm;
+                if (r == 0) hm = shn[nr][nc];
+                else if (r == R) hm = shn[nr - 1][nc];
+                else hm = sw2d_half(shn[nr][nc] + shn[nr - 1][nc]);
+                p.uu1[i] = sw2d_ge_pos(hm, th) ? (sw2d_is0(F) ? F : F / hm) : 0.00; /* 0/hm is 0 of F's sign */
+            }
+            if (r < R) {
+                double F = fy[i];
+                if ((sw2d_gt0(F) && sdry[dr][dc - 1]) || (sw2d_lt0(F) && sdry[dr][dc])) {
+                    F = 0;
+                    p.qy[nxt][i] = F;
+                }
+                double hn;
+                if (c == 0) hn = shn[nr][nc];
+                else if (c == C) hn = shn[nr][nc - 1];
+                else hn = sw2d_half(shn[nr][nc] + shn[nr][nc - 1]);
+                p.vv1[i] = sw2d_ge_pos(hn, th) ? (sw2d_is0(F) ? F : F / hn) : 0.0;
             }
         }
     }
+    /* ledger partials of the tile, then the last block's reduction */
     double pr = 0.0, pe = 0.0, pq = 0.0;
     if (p.ledger_cells) {
         pr = block_sum(vr, smd);
         pe = block_sum(ve, smd);
     }
-    if (p.outflow_south && (blockIdx.y + 1) * SW2D_BY >= p.R) pq = block_sum(vq, smd);
-    const int tid = tid_linear();
+    if (p.outflow_south) pq = block_sum(vq, smd);
     const int b = blockIdx.y * gridDim.x + blockIdx.x;
     if (tid == 0) {
         double* pb = p.partials + (size_t)b * NPART;
@@ -698,25 +766,20 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int
 }
 
 /* ------------------------------------------------------------------------ */
-/* hm_hn + uu1_vv1: SW2D-EFDC.cu:362-452, with the closed faces written back  */
+/* hm_hn + uu1_vv1: SW2D-EFDC.cu:362-452, the face velocities of the current
+ * state (after its depth was set or restored; the iteration's own are
+ * written by k64_update) */
 
-__global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, int cur, int clip) {
+__global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, int cur) {
     const int c = blockIdx.x * SW2D_BX + threadIdx.x;
     const int r = blockIdx.y * SW2D_BY + threadIdx.y;
     if (r > p.R || c > p.C) return;
-    const int nxt = clip ? (cur ^ 1) : cur;
-    if (clip && !p.clk->slot[cur].active) return;
     const int P = p.P;
     const size_t i = (size_t)(r + H) * P + (c + H);
-    const double* __restrict__ h = p.h[nxt];
-    const uint8_t* __restrict__ d = p.drys;
+    const double* __restrict__ h = p.h[cur];
     const double th = p.th;
     if (c < p.C) {
-        double F = p.qx[nxt][i];
-        if (clip && ((sw2d_gt0(F) && d[i - P]) || (sw2d_lt0(F) && d[i]))) {
-            F = 0;
-            p.qx[nxt][i] = F;
-        }
+        const double F = p.qx[cur][i];
         double hm;
         if (r == 0) hm = h[i];
         else if (r == p.R) hm = h[i - P];
@@ -724,11 +787,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, i
         p.uu1[i] = sw2d_ge_pos(hm, th) ? (sw2d_is0(F) ? F : F / hm) : 0.00; /* 0/hm is 0 of F's sign */
     }
     if (r < p.R) {
-        double F = p.qy[nxt][i];
-        if (clip && ((sw2d_gt0(F) && d[i - 1]) || (sw2d_lt0(F) && d[i]))) {
-            F = 0;
-            p.qy[nxt][i] = F;
-        }
+        const double F = p.qy[cur][i];
         double hn;
         if (c == 0) hn = h[i];
         else if (c == p.C) hn = h[i - 1];
@@ -805,19 +864,16 @@ static dim3 grid_cells(const StepParams& p) {
     return dim3((p.C + SW2D_BX - 1) / SW2D_BX, (p.R + SW2D_BY - 1) / SW2D_BY);
 }
 
-int fp64_kernels_per_iteration() { return 4; }
+int fp64_kernels_per_iteration() { return 2; }
 
 void fp64_launch_iteration(const StepParams& p, int cur, cudaStream_t s, cudaEvent_t* ev) {
     const dim3 blk(SW2D_BX, SW2D_BY);
     if (ev) cudaEventRecord(ev[0], s);
     k64_flux<<<grid_faces(p), blk, 0, s>>>(p, cur);
     if (ev) cudaEventRecord(ev[1], s);
-    k64_hstar<<<grid_cells(p), blk, 0, s>>>(p, cur);
+    const dim3 gu((p.C + 1 + UT_W - 1) / UT_W, (p.R + 1 + UT_H - 1) / UT_H);
+    k64_update<<<gu, SW2D_BX * SW2D_BY, 0, s>>>(p, cur);
     if (ev) cudaEventRecord(ev[2], s);
-    k64_depth<<<grid_cells(p), blk, 0, s>>>(p, cur);
-    if (ev) cudaEventRecord(ev[3], s);
-    k64_facevel<<<grid_faces(p), blk, 0, s>>>(p, cur, 1);
-    if (ev) cudaEventRecord(ev[4], s);
 }
 
 void fp64_launch_prime(const StepParams& p, int cur, int full, cudaStream_t s) {
@@ -825,7 +881,7 @@ void fp64_launch_prime(const StepParams& p, int cur, int full, cudaStream_t s) {
 }
 
 void fp64_launch_face_velocity(const StepParams& p, int cur, cudaStream_t s) {
-    k64_facevel<<<grid_faces(p), dim3(SW2D_BX, SW2D_BY), 0, s>>>(p, cur, 0);
+    k64_facevel<<<grid_faces(p), dim3(SW2D_BX, SW2D_BY), 0, s>>>(p, cur);
 }
 
 void fp64_launch_cell_velocity(const StepParams& p, int cur, double* uu, double* vv, double* uua,

@@ -96,7 +96,6 @@ struct StepParams {
     double* qy[2];
     double* uu1;
     double* vv1;
-    uint8_t* drys;
     double* partials;      /* nblocks_cells * 4: rain, evaporation, outlet sums */
     double* partials_f;    /* nblocks_faces * 2: CFL face-speed maxima (bit patterns) */
     int nblocks_faces;
