@@ -559,7 +559,7 @@ def run_served_leg(args, fp64_value):
         for rid, k in list(ids.items()):
             if k in done:
                 continue
-            st, _ = b.poll(rid)
+            st, _ = b.poll(rid, ledger=False)
             if st in (api.REQ_RUNNING, api.REQ_DONE) and k not in admitted:
                 admitted[k] = t_step  # admitted at the start of this step
             if st == api.REQ_DONE:

@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-#define SW2D_ABI_VERSION 1
+#define SW2D_ABI_VERSION 2
 
 /* Status codes.  The reference checks no error at all (no cudaGetLastError,
  * missing files print and return 0, SW2D-EFDC.cu:3757-3761). */

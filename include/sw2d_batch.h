@@ -53,11 +53,13 @@ typedef struct sw2d_scenario {
 typedef struct sw2d_batch_stats {
     int running, queued;
     int work_items;           /* tiles per iteration */
-    int reserved;
+    int rows_per_item;        /* rows of a work item in use (the autotuner's choice unless set) */
     double bytes_in_use;
     double device_ms;         /* device time of all iterations so far */
     double cell_updates;      /* sum over scenarios of cells x iterations advanced */
-    double launches;          /* kernel launches issued */
+    double launches;          /* kernel launches issued (one persistent launch per feature class and chunk) */
+    double tuning_ms;         /* host time the autotuner spent timing candidate work items (its timed
+                                 iterations advanced the scenarios like any other) */
 } sw2d_batch_stats;
 
 typedef struct sw2d_batch sw2d_batch;
@@ -69,17 +71,21 @@ int sw2d_batch_submit(sw2d_batch* b, const sw2d_scenario* s, int64_t* id_out);
 /* Admit what fits, advance every running scenario by `iterations`
  * iterations, retire the finished ones. */
 int sw2d_batch_step(sw2d_batch* b, int iterations, int* n_running_out, int* n_queued_out);
+/* Status of a request and its ledger: as of now for a running request
+ * (read from the device: time, iterations, volumes so far), final for a
+ * finished one, zeros for a queued one. */
 int sw2d_batch_poll(sw2d_batch* b, int64_t id, int* status, sw2d_ledger* ledger);
 /* Final fields of a finished request: depth rows*cols, qx (rows+1)*cols,
  * qy rows*(cols+1), reference orientation; any pointer may be NULL. */
 int sw2d_batch_result(sw2d_batch* b, int64_t id, double* depth, double* qx, double* qy);
 int sw2d_batch_release(sw2d_batch* b, int64_t id);
-/* Rows per work item of the scenarios admitted from now on; 0 (the default)
- * chooses per raster: 128 below 1 Mcell, the autotuned value above.  A batch
- * whose scenarios arrive together runs faster with 256 (fewer halo rows; the
- * number of scenarios supplies the parallelism); a serving loop with few
- * scenarios at a time needs the default's shorter items.  The choice fixes
- * each scenario's tiling, so its results do not depend on the others. */
+/* Rows per work item (a multiple of 4 in 16..512) for every scenario of the
+ * batch; 0 (the default) lets the autotuner choose: when the batch's cells
+ * first reach 1 M, and again when they have halved or doubled since, it
+ * times 64, 128, 256 and 512 rows on three of the scenarios' own iterations
+ * each and keeps the fastest.  Results do not depend on the choice (the bed's
+ * datum tiles are fixed at 224 columns x 64 rows), so a scenario's results
+ * are the same alone and in any mix. */
 int sw2d_batch_set_rows_per_item(sw2d_batch* b, int rows);
 int sw2d_batch_get_stats(sw2d_batch* b, sw2d_batch_stats* out);
 const char* sw2d_batch_last_error(void);

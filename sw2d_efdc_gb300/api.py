@@ -71,9 +71,9 @@ class Scenario(C.Structure):
 
 
 class BatchStats(C.Structure):
-    _fields_ = [("running", C.c_int), ("queued", C.c_int), ("work_items", C.c_int), ("reserved", C.c_int),
+    _fields_ = [("running", C.c_int), ("queued", C.c_int), ("work_items", C.c_int), ("rows_per_item", C.c_int),
                 ("bytes_in_use", C.c_double), ("device_ms", C.c_double), ("cell_updates", C.c_double),
-                ("launches", C.c_double)]
+                ("launches", C.c_double), ("tuning_ms", C.c_double)]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
@@ -452,11 +452,14 @@ class Batch:
         _bcheck(load().sw2d_batch_step(self._h, int(iterations), C.byref(nr), C.byref(nq)), "sw2d_batch_step")
         return nr.value, nq.value
 
-    def poll(self, rid):
+    def poll(self, rid, ledger=True):
+        """(status, ledger dict); with ledger=False only the status (no
+        device read for a running request) and None."""
         st = C.c_int(0)
         L = Ledger()
-        _bcheck(load().sw2d_batch_poll(self._h, int(rid), C.byref(st), C.byref(L)), "sw2d_batch_poll")
-        return st.value, {n: getattr(L, n) for n, _ in Ledger._fields_}
+        _bcheck(load().sw2d_batch_poll(self._h, int(rid), C.byref(st), C.byref(L) if ledger else None),
+                "sw2d_batch_poll")
+        return st.value, ({n: getattr(L, n) for n, _ in Ledger._fields_} if ledger else None)
 
     def result(self, rid):
         R, Cc = self._shapes[rid]
@@ -471,7 +474,8 @@ class Batch:
         _bcheck(load().sw2d_batch_release(self._h, int(rid)), "sw2d_batch_release")
 
     def set_rows_per_item(self, rows):
-        """Rows per work item of scenarios admitted from now on (0 = default)."""
+        """Rows per work item, 16..512 (0 = the autotuner's choice); results
+        do not depend on it."""
         _bcheck(load().sw2d_batch_set_rows_per_item(self._h, int(rows)), "sw2d_batch_set_rows_per_item")
 
     def stats(self) -> dict:

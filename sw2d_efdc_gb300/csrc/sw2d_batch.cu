@@ -109,21 +109,16 @@ static sw2d::ScenarioInput to_input(const Request& r) {
     return in;
 }
 
-static int retire(sw2d_batch* b, size_t k) {
-    const int64_t id = b->running[k];
-    Request& r = *b->reqs[id];
+/* the ledger of the scenario at engine index k, from its device clock and
+ * a volume measure of its current state */
+static int read_ledger(sw2d_batch* b, size_t k, sw2d_ledger* out, sw2d::Clock32* clock_out) {
     std::string err;
-    const size_t n = (size_t)r.desc.rows * r.desc.cols;
-    r.r_depth.resize(n);
-    r.r_qx.resize((size_t)(r.desc.rows + 1) * r.desc.cols);
-    r.r_qy.resize((size_t)r.desc.rows * (r.desc.cols + 1));
-    int rc = b->eng->get_state((int)k, r.r_depth.data(), r.r_qx.data(), r.r_qy.data(), &err);
-    if (rc) return bfail(rc, err);
     sw2d::Clock32 c;
     double vol = 0, smax = 0;
+    int rc;
     if ((rc = b->eng->get_clock((int)k, &c, &err))) return bfail(rc, err);
     if ((rc = b->eng->get_volume((int)k, &vol, &smax, &err))) return bfail(rc, err);
-    sw2d_ledger& L = r.ledger;
+    sw2d_ledger& L = *out;
     L.time = c.t;
     L.iterations = (double)c.iters;
     L.volume = vol;
@@ -139,6 +134,22 @@ static int retire(sw2d_batch* b, size_t k) {
     const double inflow = L.rain_in + L.source_in;
     L.balance_error = (L.volume - L.volume0 - L.rain_in - L.source_in + L.evap_out + L.outflow) /
                       std::max(std::fabs(inflow), 1e-300);
+    if (clock_out) *clock_out = c;
+    return SW2D_OK;
+}
+
+static int retire(sw2d_batch* b, size_t k) {
+    const int64_t id = b->running[k];
+    Request& r = *b->reqs[id];
+    std::string err;
+    const size_t n = (size_t)r.desc.rows * r.desc.cols;
+    r.r_depth.resize(n);
+    r.r_qx.resize((size_t)(r.desc.rows + 1) * r.desc.cols);
+    r.r_qy.resize((size_t)r.desc.rows * (r.desc.cols + 1));
+    int rc = b->eng->get_state((int)k, r.r_depth.data(), r.r_qx.data(), r.r_qy.data(), &err);
+    if (rc) return bfail(rc, err);
+    sw2d::Clock32 c;
+    if ((rc = read_ledger(b, k, &r.ledger, &c))) return rc;
     r.iterations = c.iters;
     r.status = (c.status & 3) ? SW2D_REQ_FAILED : SW2D_REQ_DONE;
     b->eng->remove((int)k);
@@ -271,7 +282,8 @@ int sw2d_batch_step(sw2d_batch* b, int iterations, int* n_running_out, int* n_qu
         int rc = b->eng->run(iterations, &err);
         if (rc) return bfail(rc, err);
         b->device_ms += b->eng->last_ms();
-        b->launches += (long long)iterations * b->eng->launches_per_iteration();
+        b->launches += (long long)((iterations + sw2d::Engine32::kChunk - 1) / sw2d::Engine32::kChunk) *
+                       b->eng->launches_per_chunk();
         /* retire finished scenarios (highest index first keeps indices valid) */
         for (size_t k = b->running.size(); k-- > 0;) {
             sw2d::Clock32 c;
@@ -297,7 +309,14 @@ int sw2d_batch_poll(sw2d_batch* b, int64_t id, int* status, sw2d_ledger* ledger)
     if (it == b->reqs.end()) return bfail(SW2D_ERR_NOT_FOUND, "unknown request id");
     Request& r = *it->second;
     if (status) *status = r.status;
-    if (ledger) *ledger = r.ledger;
+    if (ledger) {
+        if (r.status == SW2D_REQ_RUNNING) {
+            /* a running request's ledger as of now, read from the device */
+            for (size_t k = 0; k < b->running.size(); k++)
+                if (b->running[k] == id) return read_ledger(b, k, ledger, nullptr);
+        }
+        *ledger = r.ledger;
+    }
     return SW2D_OK;
 }
 
@@ -336,8 +355,8 @@ int sw2d_batch_release(sw2d_batch* b, int64_t id) {
 
 int sw2d_batch_set_rows_per_item(sw2d_batch* b, int rows) {
     if (!b) return bfail(SW2D_ERR_INVALID, "null batch");
-    if (rows != 0 && (rows < 16 || rows > 4096 || rows % 4 != 0))
-        return bfail(SW2D_ERR_INVALID, "rows per work item: 0, or a multiple of 4 in 16..4096");
+    if (rows != 0 && (rows < 16 || rows > sw2d::M_MAXSEG || rows % 4 != 0))
+        return bfail(SW2D_ERR_INVALID, "rows per work item: 0, or a multiple of 4 in 16..512");
     b->eng->set_segment_rows(rows);
     return SW2D_OK;
 }
@@ -351,6 +370,8 @@ int sw2d_batch_get_stats(sw2d_batch* b, sw2d_batch_stats* out) {
     out->cell_updates = b->cell_updates;
     out->launches = (double)b->launches;
     out->work_items = b->eng->nwork();
+    out->rows_per_item = b->eng->segment_rows();
+    out->tuning_ms = b->eng->tuning_ms();
     return SW2D_OK;
 }
 

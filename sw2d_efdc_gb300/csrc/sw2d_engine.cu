@@ -4,6 +4,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -14,7 +15,6 @@ namespace sw2d {
 
 namespace {
 
-constexpr int kChunk32 = 16; /* iterations per captured graph */
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
@@ -67,9 +67,12 @@ Engine32::~Engine32() {
     cudaFree(d_scn_);
     cudaFree(d_work_);
     cudaFree(d_part_);
+    cudaFree(d_ctl_);
     cudaFree(d_tmp_);
     if (ev_a_) cudaEventDestroy(ev_a_);
     if (ev_b_) cudaEventDestroy(ev_b_);
+    if (ev_t0_) cudaEventDestroy(ev_t0_);
+    if (ev_t1_) cudaEventDestroy(ev_t1_);
     if (stream_) cudaStreamDestroy(stream_);
     if (pin_) cudaFreeHost(pin_);
 }
@@ -84,9 +87,22 @@ int Engine32::init(std::string* err) {
         if (err) *err = "cannot enable the FP32 kernel's shared memory";
         return SW2D_ERR_CUDA;
     }
-    /* rows per work item: SW2D_SEGMENT_ROWS overrides the default (tuning knob) */
-    if (seg_rows_ == 0) {
-        if (const char* e = std::getenv("SW2D_SEGMENT_ROWS")) seg_rows_ = std::max(0, std::atoi(e));
+    /* rows per work item: SW2D_SEGMENT_ROWS fixes it (else the autotuner) */
+    if (seg_fixed_ == 0) {
+        if (const char* e = std::getenv("SW2D_SEGMENT_ROWS")) {
+            const int v = std::atoi(e);
+            if (v >= 16 && v <= M_MAXSEG) seg_ = seg_fixed_ = v;
+        }
+    }
+    ECK(cudaEventCreate(&ev_t0_));
+    ECK(cudaEventCreate(&ev_t1_));
+    ECK(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, device_));
+    for (int k = 0; k < T32_NCLASS; k++) {
+        bps_[k] = fp32_blocks_per_sm(k);
+        if (bps_[k] <= 0) {
+            if (err) *err = "the FP32 kernel does not fit on an SM";
+            return SW2D_ERR_CUDA;
+        }
     }
     if (!encode_fn()) {
         if (err) *err = "cuTensorMapEncodeTiled unavailable";
@@ -103,61 +119,6 @@ size_t Engine32::scenario_bytes(int rows, int cols, bool rain_field, int outlet_
     const size_t tiles = (size_t)((cols + M_CW - 1) / M_CW) * ((rows + 15) / 16);
     b += tiles * sizeof(float) + (size_t)outlet_cap * 16 + sizeof(Clock32) + 4096;
     return b;
-}
-
-int Engine32::segment_rows_for(int rows, int cols) {
-    if (seg_rows_ > 0) return seg_rows_;
-    if (tuning_) return 128;
-    if ((long long)rows * cols <= small_cells_) return small_seg_;
-    auto bucket = [](int n) {
-        int b = 0;
-        while ((1 << b) < n) b++;
-        return b;
-    };
-    const std::pair<int, int> key(bucket(rows), bucket(cols));
-    auto it = seg_cache_.find(key);
-    if (it != seg_cache_.end()) return it->second;
-    /* time the candidates on a scratch scenario of the bucket's size: a wet
-     * 1% plane with gentle bumps, CFL steps; skipped (128) when the device
-     * has no room for it */
-    const int tr = 1 << key.first, tc = 1 << key.second;
-    int best = 128;
-    size_t fr = 0, tot = 0;
-    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > 3 * scenario_bytes(tr, tc, false, 0)) {
-        std::vector<double> dem((size_t)tr * tc), depth((size_t)tr * tc, 0.05);
-        for (int r = 0; r < tr; r++)
-            for (int c = 0; c < tc; c++)
-                dem[(size_t)r * tc + c] = 0.01 * (tr - 1 - r) + 0.05 * std::sin(0.05 * c) * std::cos(0.03 * r);
-        const double rain0 = 0.0;
-        ScenarioInput in;
-        in.rows = tr;
-        in.cols = tc;
-        in.dem = dem.data();
-        in.depth = depth.data();
-        in.rain = &rain0;
-        in.nrain = 1;
-        in.t_end = 1e9;
-        double best_ms = 1e300;
-        for (int cand : {64, 128, 256, 512}) {
-            if (cand > 2 * tr) continue;
-            Engine32 scratch(device_);
-            std::string e2;
-            scratch.tuning_ = true;
-            scratch.seg_rows_ = cand;
-            int idx = -1;
-            if (scratch.init(&e2) || scratch.add(in, 0, &e2, &idx) || scratch.set_t_end(-1, 1e9, &e2) ||
-                scratch.run(4, &e2) || scratch.run(8, &e2))
-                break;
-            const double ms = scratch.last_ms();
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = cand;
-            }
-        }
-        cudaSetDevice(device_);
-    }
-    seg_cache_[key] = best;
-    return best;
 }
 
 size_t Engine32::bytes_in_use() const {
@@ -185,8 +146,7 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     S.P = P;
     S.NR = NR;
     const size_t cells = (size_t)P * NR;
-    const int seg = segment_rows_for(R, C);
-    const int tx = (C + M_CW - 1) / M_CW, ty = (R + seg - 1) / seg;
+    const int tx = (C + M_CW - 1) / M_CW, nb = (R + M_DR - 1) / M_DR; /* datum tiles: strips x bands */
     auto alloc = [&](size_t bytes, void** p) -> int {
         cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
         if (e != cudaSuccess) {
@@ -227,7 +187,7 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     }
     d.cls = dcls;
     float* ddatum;
-    if ((rc = alloc((size_t)tx * ty * 4, &p))) return fail_free(rc);
+    if ((rc = alloc((size_t)tx * nb * 4, &p))) return fail_free(rc);
     ddatum = (float*)p;
     d.datum = ddatum;
     float* drw = nullptr;
@@ -286,18 +246,19 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     dclk = (Clock32*)p;
     d.clk = dclk;
 
-    /* host staging: per-tile datum (a multiple of 1/16 m) over the kernel's
-     * (strip, segment) tiles, bed offsets with NaN for inactive cells */
-    std::vector<float> datum((size_t)tx * ty, 0.f);
+    /* host staging: per datum tile (a strip of 224 columns x a band of 64
+     * rows) the mean active elevation rounded to 1/16 m, bed offsets from it
+     * with NaN for inactive cells */
+    std::vector<float> datum((size_t)tx * nb, 0.f);
     std::vector<float> zoff(cells, std::numeric_limits<float>::quiet_NaN()), hbuf(cells, 0.f), rw;
     std::vector<uint8_t> cls;
     if (in.mclass) cls.assign(cells, 0);
     double active_weight = 0.0;
-    for (int j = 0; j < ty; j++)
+    for (int j = 0; j < nb; j++)
         for (int i = 0; i < tx; i++) {
             double sum = 0;
             long n = 0;
-            for (int r = j * seg; r < std::min(R, (j + 1) * seg); r++)
+            for (int r = j * M_DR; r < std::min(R, (j + 1) * M_DR); r++)
                 for (int c = i * M_CW; c < std::min(C, (i + 1) * M_CW); c++) {
                     double z = in.dem[(size_t)r * C + c];
                     if (z != in.nodata) {
@@ -314,7 +275,7 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
             const size_t g = (size_t)(r + M_H) * P + (c + M_H);
             const double z = in.dem[k];
             const bool act = z != in.nodata;
-            const double dat = datum[(size_t)(r / seg) * tx + (c / M_CW)];
+            const double dat = datum[(size_t)(r / M_DR) * tx + (c / M_CW)];
             if (act) zoff[g] = (float)(z - dat);
             if (in.mclass) {
                 const uint8_t cl = in.mclass[k];
@@ -373,8 +334,9 @@ int Engine32::add(const ScenarioInput& in, long long id, std::string* err, int* 
     d.C = C;
     d.P = P;
     d.tiles_x = tx;
-    d.tiles_y = ty;
-    d.seg = seg;
+    d.bands = nb;
+    d.seg = 0;     /* work items: set by rebuild */
+    d.tiles_y = 0;
     d.outflow_south = in.outflow_south;
     d.series_mode = in.series_mode;
     d.dt_mode = in.dt_mode;
@@ -444,24 +406,27 @@ int Engine32::rebuild(std::string* err) {
     if (!dirty_) return SW2D_OK;
     work_.clear();
     std::vector<Scn32> host(scn_.size());
-    /* work items grouped by feature class, scenarios in order within a class */
+    /* work items grouped by feature class, scenarios in order within a class;
+     * .w is the item's slot in the scenario-ordered partials */
     for (int k = 0; k < T32_NCLASS; k++) {
         class_first_[k] = (int)work_.size();
         for (size_t i = 0; i < scn_.size(); i++) {
             Scn32& d = scn_[i]->d;
             if (fp32_feature_class(d) != k) continue;
+            d.seg = std::min(seg_, d.R);
+            d.tiles_y = (d.R + d.seg - 1) / d.seg;
             d.first_work = (int)work_.size();
             for (int ty = 0; ty < d.tiles_y; ty++)
                 for (int tx = 0; tx < d.tiles_x; tx++)
-                    work_.push_back(make_int4((int)i, tx, ty, (int)work_.size() - class_first_[k]));
+                    work_.push_back(make_int4((int)i, tx, ty, (int)work_.size()));
             d.nwork = (int)work_.size() - d.first_work;
             host[i] = d;
         }
         class_n_[k] = (int)work_.size() - class_first_[k];
-        /* launch the class's longest work items first (a scenario's last
-         * segment is shorter), so that the last wave of CTAs is not left
-         * with long items; .w keeps each item's slot in the scenario-ordered
-         * partials that k32_finalize reduces */
+        /* the class's longest items first in every iteration (a scenario's
+         * last segment is shorter), so the tail of an iteration holds short
+         * items; the order is the same in every iteration, so a scenario's
+         * items of the next iteration come after its own of this one */
         auto rows_of = [&](const int4& w) {
             const Scn32& d = scn_[w.x]->d;
             return std::min(d.seg, d.R - w.z * d.seg);
@@ -484,6 +449,12 @@ int Engine32::rebuild(std::string* err) {
         ECK(cudaMalloc(&d_work_, d_work_cap_ * sizeof(int4)));
         ECK(cudaMalloc(&d_part_, d_work_cap_ * sizeof(Part32)));
     }
+    if (fp32_ctl_bytes((int)scn_.size()) > d_ctl_cap_) {
+        cudaFree(d_ctl_);
+        d_ctl_ = nullptr;
+        d_ctl_cap_ = std::max(fp32_ctl_bytes((int)scn_.size()), 2 * d_ctl_cap_);
+        ECK(cudaMalloc(&d_ctl_, d_ctl_cap_));
+    }
     if (!host.empty())
         ECK(cudaMemcpyAsync(d_scn_, host.data(), host.size() * sizeof(Scn32), cudaMemcpyHostToDevice, stream_));
     if (!work_.empty())
@@ -497,19 +468,77 @@ int Engine32::rebuild(std::string* err) {
     return SW2D_OK;
 }
 
+/* niter iterations: one persistent launch per feature class present, each
+ * with as many CTAs as its SMs hold (at most one per queue ticket) */
+int Engine32::launch(int niter, std::string* err) {
+    int grid[T32_NCLASS];
+    for (int k = 0; k < T32_NCLASS; k++)
+        grid[k] = (int)std::max<long long>(1, std::min<long long>((long long)bps_[k] * nsm_, (long long)class_n_[k] * niter));
+    ECK(fp32_launch_chunk(d_scn_, (int)scn_.size(), d_work_, class_first_, class_n_, d_part_, d_ctl_, niter, grid,
+                          stream_));
+    return SW2D_OK;
+}
+
 int Engine32::build_graph(std::string* err) {
-    if (graph_) return SW2D_OK;
-    cudaGraph_t g;
+    if (graph_ || graph_failed_) return SW2D_OK;
+    cudaGraph_t g = nullptr;
     ECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < kChunk32; k++)
-        fp32_launch_iteration(d_scn_, (int)scn_.size(), d_work_, class_first_, class_n_, d_part_, stream_);
-    ECK(cudaStreamEndCapture(stream_, &g));
-    cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) {
-        if (err) *err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e);
-        return SW2D_ERR_CUDA;
+    int grid[T32_NCLASS];
+    for (int k = 0; k < T32_NCLASS; k++)
+        grid[k] = (int)std::max<long long>(1, std::min<long long>((long long)bps_[k] * nsm_, (long long)class_n_[k] * kChunk));
+    cudaError_t el = fp32_launch_chunk(d_scn_, (int)scn_.size(), d_work_, class_first_, class_n_, d_part_, d_ctl_, kChunk,
+                                       grid, stream_);
+    cudaError_t ec = cudaStreamEndCapture(stream_, &g);
+    cudaError_t ei = cudaErrorUnknown;
+    if (el == cudaSuccess && ec == cudaSuccess && g) ei = cudaGraphInstantiate(&graph_, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        /* a cooperative launch the capture could not take: the chunks are
+         * launched directly (one launch per 32 iterations either way) */
+        graph_ = nullptr;
+        graph_failed_ = true;
+        cudaGetLastError();
     }
+    return SW2D_OK;
+}
+
+int Engine32::tune(std::string* err, long long* advanced) {
+    *advanced = 0;
+    double cells = 0;
+    for (auto& sp : scn_) cells += (double)sp->R * sp->C;
+    if (seg_fixed_ > 0 || cells < (1 << 20)) return SW2D_OK;
+    if (tuned_cells_ > 0 && cells <= 2.0 * tuned_cells_ && cells >= 0.5 * tuned_cells_) return SW2D_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    int best = seg_;
+    float best_ms = 3.4e38f;
+    int rc;
+    for (int cand : {64, 128, 256, 512}) {
+        if (cand != seg_) {
+            seg_ = cand;
+            dirty_ = true;
+            if ((rc = rebuild(err))) return rc;
+        }
+        if ((rc = launch(1, err))) return rc;
+        ECK(cudaEventRecord(ev_t0_, stream_));
+        if ((rc = launch(2, err))) return rc;
+        ECK(cudaEventRecord(ev_t1_, stream_));
+        ECK(cudaEventSynchronize(ev_t1_));
+        float ms = 0;
+        ECK(cudaEventElapsedTime(&ms, ev_t0_, ev_t1_));
+        *advanced += 3;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = cand;
+        }
+    }
+    if (best != seg_) {
+        seg_ = best;
+        dirty_ = true;
+        if ((rc = rebuild(err))) return rc;
+    }
+    tuned_cells_ = cells;
+    tuning_ms_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    tunings_++;
     return SW2D_OK;
 }
 
@@ -535,11 +564,19 @@ int Engine32::run(long long n, std::string* err) {
     int rc = rebuild(err);
     if (rc) return rc;
     if (scn_.empty() || n <= 0) return SW2D_OK;
-    if ((rc = build_graph(err))) return rc;
     ECK(cudaEventRecord(ev_a_, stream_));
-    for (long long k = 0; k < n / kChunk32; k++) ECK(cudaGraphLaunch(graph_, stream_));
-    for (long long k = 0; k < n % kChunk32; k++)
-        fp32_launch_iteration(d_scn_, (int)scn_.size(), d_work_, class_first_, class_n_, d_part_, stream_);
+    long long done = 0;
+    if (n >= 16) {
+        if ((rc = tune(err, &done))) return rc;
+    }
+    if ((rc = build_graph(err))) return rc;
+    for (; n - done >= kChunk; done += kChunk) {
+        if (graph_)
+            ECK(cudaGraphLaunch(graph_, stream_));
+        else if ((rc = launch(kChunk, err)))
+            return rc;
+    }
+    if (n > done && (rc = launch((int)(n - done), err))) return rc;
     ECK(cudaGetLastError());
     ECK(cudaEventRecord(ev_b_, stream_));
     ECK(cudaEventSynchronize(ev_b_));

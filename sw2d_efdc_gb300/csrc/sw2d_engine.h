@@ -9,7 +9,6 @@
 
 #include <nvtx3/nvToolsExt.h>
 
-#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -97,33 +96,43 @@ class Engine32 {
     double last_ms() const { return last_ms_; }
     long long last_iters() const { return last_iters_; }
     int nwork() const { return (int)work_.size(); }
-    /* kernel launches of one iteration of the current work list: one
-     * row-marching launch per feature class present, then the finalize */
-    int launches_per_iteration() const {
-        int n = 1;
+    /* kernel launches of one chunk of iterations: one persistent launch per
+     * feature class present */
+    int launches_per_chunk() const {
+        int n = 0;
         for (int k = 0; k < T32_NCLASS; k++) n += class_n_[k] > 0 ? 1 : 0;
         return n;
     }
+    /* iterations one chunk (one persistent launch per class) advances */
+    static constexpr int kChunk = 32;
     int sync(std::string* err);
-    /* rows per work item of scenarios added from now on (0 = chosen by
-     * segment_rows_for) */
-    void set_segment_rows(int rows) { seg_rows_ = rows; }
-    /* rows per work item of rasters of at most `cells` cells (by default 128
-     * below 1 Mcell: a lone small raster needs the parallelism, a batch of
-     * many has it anyway); larger rasters use the autotuned choice */
-    void set_small_segment_rows(int rows, long long cells) {
-        small_seg_ = rows;
-        small_cells_ = cells;
+    /* rows per work item (16..512; 0 = chosen by the autotuner).  The
+     * results do not depend on it: the bed's datum tiles are fixed. */
+    void set_segment_rows(int rows) {
+        seg_fixed_ = rows;
+        if (rows > 0 && rows != seg_) {
+            seg_ = rows;
+            dirty_ = true;
+        }
+        tuned_cells_ = 0;
     }
-    /* Rows per work item for a raster of this size: the fixed value when one
-     * is set, else the autotuned choice (timed once per power-of-two size
-     * bucket on a scratch scenario) for rasters of >= 1 Mcell, else 128. */
-    int segment_rows_for(int rows, int cols);
+    int segment_rows() const { return seg_; }
+    /* host milliseconds the autotuner spent timing candidates (the
+     * iterations it timed were real ones: they advanced the scenarios) */
+    double tuning_ms() const { return tuning_ms_; }
+    int tunings() const { return tunings_; }
 
   private:
     int rebuild(std::string* err);
     int build_graph(std::string* err);
+    int launch(int niter, std::string* err);
+    /* the autotuner: times each candidate rows-per-item on two of the
+     * scenarios' own iterations (after one untimed) and keeps the fastest;
+     * returns the iterations it advanced */
+    int tune(std::string* err, long long* advanced);
     int device_;
+    int nsm_ = 0;
+    int bps_[T32_NCLASS] = {};  /* CTAs per SM of each class's persistent kernel */
     cudaStream_t stream_ = nullptr;
     std::vector<std::unique_ptr<Scenario32>> scn_;
     std::vector<int4> work_;
@@ -133,21 +142,22 @@ class Engine32 {
     int4* d_work_ = nullptr;
     size_t d_work_cap_ = 0;
     Part32* d_part_ = nullptr;
-    size_t d_part_cap_ = 0;
+    void* d_ctl_ = nullptr;    /* persistent-launch control block, fp32_ctl_bytes */
+    size_t d_ctl_cap_ = 0;
     double* d_tmp_ = nullptr;
     bool dirty_ = true;
     cudaGraphExec_t graph_ = nullptr;
-    int graph_iters_ = 0;
-    cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr;
+    bool graph_failed_ = false; /* capture of the cooperative launch refused: launch directly */
+    cudaEvent_t ev_a_ = nullptr, ev_b_ = nullptr, ev_t0_ = nullptr, ev_t1_ = nullptr;
     double last_ms_ = 0.0;
     long long last_iters_ = 0;
-    int seg_rows_ = 0;
-    int small_seg_ = 128;
-    long long small_cells_ = (1ll << 20) - 1;
+    int seg_ = 128;            /* rows per work item in use */
+    int seg_fixed_ = 0;        /* set by set_segment_rows or SW2D_SEGMENT_ROWS */
+    double tuned_cells_ = 0;   /* cells of the work set the last tuning saw */
+    double tuning_ms_ = 0.0;
+    int tunings_ = 0;
     void* pin_ = nullptr;      /* pinned staging of state downloads */
     size_t pin_bytes_ = 0;
-    bool tuning_ = false;                       /* a scratch engine of the autotuner */
-    std::map<std::pair<int, int>, int> seg_cache_; /* size bucket -> tuned rows per work item */
 };
 
 } // namespace sw2d

@@ -57,12 +57,14 @@ struct SmemM {
     alignas(128) float stage[NS][NF][RB][BW];
     unsigned long long bar[NS];
     float ntab[T32_MAXCLASS];
-    float dd[9];
+    float dband[M_MAXBANDS][3]; /* datums of the bands the item spans, strips west / own / east */
     double red[NW][4];
     float redf[NW][2];
     int nls;                    /* point sources inside the work item's staged window */
     int srow[T32_MAXSRC], scol[T32_MAXSRC];
     float sq1[T32_MAXSRC], sq2[T32_MAXSRC];
+    unsigned q;                 /* queue ticket of the item in hand (~0u: leave) */
+    int last;                   /* this CTA finished its scenario's iteration */
     ClsStage cls[NS];
     RwStage rw[NS];
 };
@@ -204,20 +206,20 @@ __device__ __forceinline__ float2 edge2(float2 w, float2 q0, float2 q1) {
 
 /* Weir and dry-bed discharges of one face (SW2D-EFDC.cu:125-157), for the
  * faces where the water surface on one side is below the other side's bed
- * or exactly one side is wet. */
-__device__ __forceinline__ float face_special(float hw, float he, float zw, float ze, float th, float g) {
-    const float hhe = he + ze, hhw = hw + zw;
-    const bool d1a = hhe < zw, d1b = hhw < ze;
+ * or exactly one side is wet; dz = z_e - z_w is the face's bed step. */
+__device__ __forceinline__ float face_special(float hw, float he, float dz, float th, float g) {
+    const bool d1a = he + dz < 0.f, d1b = hw - dz < 0.f; /* surface e below bed w / surface w below bed e */
     const float hup = d1a ? hw : he;
     const float fw = (hup > th) ? (d1a ? 0.5440f : -0.544f) * hup * fsqrt(g * hup) : 0.f;
-    const float hh3 = fmaxf(hhe, hhw) - fmaxf(ze, zw);
+    const float hh3 = fmaxf(he + dz, hw) - fmaxf(dz, 0.f); /* higher surface above the higher bed */
     const float fd =
         ((he > 0.f) || (hw > 0.f)) ? -copysignf(0.350f, (he - th) - (hw - th)) * hh3 * fsqrt(2.f * g * hh3) : 0.f;
     return (d1a || d1b) ? fw : fd;
 }
 
 struct Face2 {
-    float2 hw, he, zw, ze; /* the two cells (w: north / west, e: south / east) */
+    float2 hw, he;         /* the two cells' depths (w: north / west, e: south / east) */
+    float2 dz;             /* bed step z_e - z_w */
     float2 q0, u0, vt;     /* old discharge, face velocity, cross velocity at the face */
     float2 conv;           /* along + across convection, already scaled */
     float2 fr;             /* -dt2/2 * g * n_face^2 */
@@ -230,7 +232,7 @@ struct Face2 {
  * only when some lane of the warp needs them. */
 __device__ __forceinline__ float2 face_flux2(const Face2& f, float th, float g, float gdt2n) {
     const float2 hm = mul2(add2(f.he, f.hw), f2(0.5f));
-    const float2 grav = mul2(mul2(f2(gdt2n), hm), add2(sub2(f.he, f.hw), sub2(f.ze, f.zw)));
+    const float2 grav = mul2(mul2(f2(gdt2n), hm), add2(sub2(f.he, f.hw), f.dz));
     const float2 sq = sqrt2(fma2(f.u0, f.u0, mul2(f.vt, f.vt)));
     float2 an = mul2(mul2(f.fr, sq), rpow_manning2(hm)); /* -dt2/2 * friction */
     an = sel2(gt2(hm, th), an, f2(0.f));
@@ -238,16 +240,15 @@ __device__ __forceinline__ float2 face_flux2(const Face2& f, float th, float g, 
     const float2 fm = mul2(num, rcp2(sub2(f2(1.f), an)));
     /* which form applies (SW2D-EFDC.cu:115-165) */
     const B2 wet = gt2(f.hw, th) | gt2(f.he, th);
-    const float2 hhe = add2(f.he, f.ze), hhw = add2(f.hw, f.zw);
-    const B2 d1a = {hhe.x < f.zw.x, hhe.y < f.zw.y};
-    const B2 d1b = {hhw.x < f.ze.x, hhw.y < f.ze.y};
+    const B2 d1a = lt2(add2(f.he, f.dz), 0.f);
+    const B2 d1b = lt2(sub2(f.hw, f.dz), 0.f);
     const B2 d2 = lt2(mul2(sub2(f.he, f2(th)), sub2(f.hw, f2(th))), 0.f);
     const B2 open = bits2(f.act) & wet;
     const B2 special = open & (d1a | d1b | d2);
     float2 F = sel2(andnot(open, special), fm, f2(0.f));
     if (__any_sync(0xffffffffu, any2(special))) {
-        const float sx = face_special(f.hw.x, f.he.x, f.zw.x, f.ze.x, th, g);
-        const float sy = face_special(f.hw.y, f.he.y, f.zw.y, f.ze.y, th, g);
+        const float sx = face_special(f.hw.x, f.he.x, f.dz.x, th, g);
+        const float sy = face_special(f.hw.y, f.he.y, f.dz.y, th, g);
         F = sel2(special, make_float2(sx, sy), F);
     }
     return F;
@@ -259,22 +260,32 @@ __device__ __forceinline__ float2 face_flux2(const Face2& f, float th, float g, 
  * LAKE: lake cells (depth > ev_wl_min) lose a different fraction of the rain
  * than land cells, or evaporate (the per-cell ledger is then kept too);
  * SRC: point sources. */
+/* The slot of a scenario's iteration, read past L1: the CTA that reduced the
+ * scenario's previous iteration (on any SM) wrote it during this launch. */
+__device__ __forceinline__ Slot32 load_slot(const Clock32* clk) {
+    Slot32 s;
+    const int4* src = reinterpret_cast<const int4*>(&clk->slot);
+    int4* dst = reinterpret_cast<int4*>(&s);
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(Slot32) / 16); k++) dst[k] = __ldcg(src + k);
+    return s;
+}
+static_assert(sizeof(Slot32) % 16 == 0 && offsetof(Clock32, slot) == 0, "slot read as int4");
+
+/* One work item: a strip of one scenario over `seg` rows, one iteration.
+ * Returns false when a staged load did not arrive in time (the status bit
+ * is set; the launch's results are void). */
 template <bool CLS, bool RW, bool LAKE, bool SRC>
-__global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scns, const int4* __restrict__ work,
-                                                   Part32* __restrict__ part) {
-    extern __shared__ unsigned char smem_raw[];
-    SmemM& S = *reinterpret_cast<SmemM*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+__device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 w, Part32* __restrict__ part) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int4 w = work[blockIdx.x];
-    const Scn32& P = scns[w.x];
     Clock32* clk = P.clk;
-    const Slot32 sl = clk->slot;
+    const Slot32 sl = load_slot(clk);
     if (!sl.active) {
         if (tid == 0) {
             Part32 zp = {};
             part[w.w] = zp;
         }
-        return;
+        return true;
     }
     const int cur = sl.cur, nxt = cur ^ 1;
     const int R = P.R, C = P.C, Pp = P.P;
@@ -285,10 +296,16 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
     const int nblk = (re - rs + 6 + RB - 1) / RB;
 
     if ((smem_addr(&S.stage[0][0][0][0]) & 127u) != 0u) {
-        if (tid == 0) atomicOr(&clk->status, 4);
-        return;
+        if (tid == 0) {
+            atomicOr(&clk->status, 4);
+            Part32 zp = {};
+            part[w.w] = zp;
+        }
+        return true; /* tile skipped, status bit 2 */
     }
     if (tid == 0) {
+        /* every load of the previous item was waited for: the barriers are
+         * idle and start again at phase 0 */
         for (int k = 0; k < NS; k++) mbar_init(&S.bar[k], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -312,20 +329,20 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 const int at = n + __popc(b & ((1u << lane) - 1u));
                 S.srow[at] = r;
                 S.scol[at] = c;
-                S.sq1[at] = clk->ql1[k];
-                S.sq2[at] = clk->ql2[k];
+                S.sq1[at] = __ldcg(&clk->ql1[k]);
+                S.sq2[at] = __ldcg(&clk->ql2[k]);
             }
             n += __popc(b);
         }
         if (lane == 0) S.nls = n;
     }
-    if (tid < 9) {
-        const int dy = tid / 3 - 1, dx = tid % 3 - 1;
-        const int ny = seg + dy, nx = strip + dx;
-        float d = 0.f;
-        if (ny >= 0 && ny < P.tiles_y && nx >= 0 && nx < P.tiles_x)
-            d = P.datum[ny * P.tiles_x + nx] - P.datum[seg * P.tiles_x + strip];
-        S.dd[tid] = d;
+    /* datums of the bands the staged rows span, for the strips west, own
+     * and east (0 outside the raster) */
+    const int b0 = max(Ls, 0) / M_DR;
+    const int nband = min(re + 2, R - 1) / M_DR - b0 + 1;
+    if (tid < 3 * nband) {
+        const int j = tid / 3, cr = tid - 3 * j, nx = strip + cr - 1;
+        S.dband[j][cr] = (nx >= 0 && nx < P.tiles_x) ? P.datum[(b0 + j) * P.tiles_x + nx] : 0.f;
     }
     __syncthreads();
     constexpr bool has_cls = CLS, has_rw = RW;
@@ -346,8 +363,11 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         if (has_cls) tma_load_2d(&S.cls[st].v[0][0], &P.tm_cls, c0, y - 2, &S.bar[st]);
         if (has_rw) tma_load_2d(&S.rw[st].v[0][0], &P.tm_rw, c0, y - 3, &S.bar[st]);
     };
-    if (tid == 0 && !P.stall_staging)
+    if (tid == 0 && !P.stall_staging) {
+        /* the staging buffers were last read by the generic proxy */
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         for (int b = 0; b < NS && b < nblk; b++) issue(b, b);
+    }
 
     /* lane geometry: staged columns sc, sc+1; global columns cg, cg+1 */
     const int sc = warp * M_SW + 2 * lane;
@@ -355,8 +375,11 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
     const bool own0 = (lane >= 2 && lane < 30) && cg < C;
     const bool own1 = (lane >= 2 && lane < 30) && cg + 1 < C;
     const int ownm = (own0 ? 1 : 0) | (own1 ? 2 : 0);
-    const int creg0 = sc < M_H ? 0 : (sc >= M_H + M_CW ? 2 : 1);
-    const int creg1 = sc + 1 < M_H ? 0 : (sc + 1 >= M_H + M_CW ? 2 : 1);
+    /* the lane's two columns lie in one datum column (strip west, own, east:
+     * strips start on even columns); the lanes whose first column starts a
+     * datum column see a datum step across their west y face */
+    const int creg = sc < M_H ? 0 : (sc >= M_H + M_CW ? 2 : 1);
+    const bool yedge = (sc == M_H || sc == M_H + M_CW) && cg > 0;
     const float th = P.th, gg = P.g;
     const float dt2 = sl.dt2, dt2dx = sl.dt2dx, dt2dy = sl.dt2dy;
     const float gdx = gg * dt2dx, gdy = gg * dt2dy;
@@ -374,15 +397,16 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
     const float2 colm = make_float2(cg == 0 ? 0.f : 1.f, cg + 1 == 0 ? 0.f : 1.f);
 
     /* register windows, slot = (row - Ls) & 3 */
-    float2 H[4], Z[4], QX[4], QY[4], U[4], UU[4], V[4], VV[4], VR[4];
-    float2 HL[4], ZL[4], EX[4], GY[4], FX[4], FY[4], FYR[4];
+    float2 H[4], DZX[4], QX[4], QY[4], U[4], UU[4], V[4], VV[4], VR[4];
+    float2 HL[4], DZY[4], EX[4], GY[4], FX[4], FY[4], FYR[4];
     int ACT[4], ACTL[4], DRY[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        H[k] = Z[k] = QX[k] = QY[k] = U[k] = UU[k] = V[k] = VV[k] = VR[k] = f2(0.f);
-        HL[k] = ZL[k] = EX[k] = GY[k] = FX[k] = FY[k] = FYR[k] = f2(0.f);
+        H[k] = DZX[k] = QX[k] = QY[k] = U[k] = UU[k] = V[k] = VV[k] = VR[k] = f2(0.f);
+        HL[k] = DZY[k] = EX[k] = GY[k] = FX[k] = FY[k] = FYR[k] = f2(0.f);
         ACT[k] = ACTL[k] = DRY[k] = 0;
     }
+    float2 Zp = f2(0.f); /* bed offsets of the row above */
     float clamp = 0.f, qout = 0.f, rainacc = 0.f, evc = 0.f;
     float sxm = 0.f, sym = 0.f;
     const int nls = SRC ? S.nls : 0;
@@ -428,7 +452,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                         }
                     }
                 }
-                return;
+                return false;
             }
         }
         const float* sh = &S.stage[st][0][0][0];
@@ -444,21 +468,30 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
             const int s0 = j & 3, s1 = (j + 3) & 3, s2 = (j + 2) & 3, s3 = (j + 1) & 3; /* L, L-1, L-2, L-3 */
             /* ---- row L from the staged block ---- */
             const float2 h0 = *reinterpret_cast<const float2*>(sh + j * BW + sc);
-            /* datum shift of the lane's two columns for rows above / inside / below the segment */
-            const int dzr = L < rs ? 0 : (L >= re ? 6 : 3);
-            const float2 z0 = add2(*reinterpret_cast<const float2*>(sz + j * BW + sc),
-                                   make_float2(S.dd[dzr + creg0], S.dd[dzr + creg1]));
+            const float2 z0 = *reinterpret_cast<const float2*>(sz + j * BW + sc); /* offsets from the band datum */
             const float2 qx0 = *reinterpret_cast<const float2*>(sqx + j * BW + sc);
             const float2 qy0 = *reinterpret_cast<const float2*>(sqy + j * BW + sc);
             H[s0] = h0;
-            Z[s0] = z0;
             QX[s0] = qx0;
             QY[s0] = qy0;
             ACT[s0] = mask2(act2(z0));
             const float2 hl = left2(h0);
             HL[s0] = hl;
-            ZL[s0] = left2(z0);
             ACTL[s0] = leftbits(ACT[s0]);
+            /* bed steps of the x face north of row L and the y faces west of
+             * its cells, plus the datum step where the face crosses a datum
+             * tile's edge (a band edge above row L, a strip edge west) */
+            const int bj = min(max(L, 0) / M_DR - b0, nband - 1);
+            float2 dzx = sub2(z0, Zp);
+            if ((L & (M_DR - 1)) == 0 && L > 0 && L < R) {
+                const float c = S.dband[bj][creg] - S.dband[bj - 1][creg];
+                dzx = add2(dzx, f2(c));
+            }
+            DZX[s0] = dzx;
+            Zp = z0;
+            float2 dzy = sub2(z0, left2(z0));
+            if (yedge) dzy.x += S.dband[bj][creg] - S.dband[bj][creg - 1];
+            DZY[s0] = dzy;
             /* ---- face velocities of row L (uu1 at the x face north, vv1 at the y face west) ---- */
             const float2 hm = (L == R) ? H[s1] : mul2(add2(h0, H[s1]), f2(0.5f));
             const float2 hn = mul2(add2(h0, hl), f2(0.5f));
@@ -489,8 +522,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 Face2 f;
                 f.hw = H[s2];
                 f.he = H[s1];
-                f.zw = Z[s2];
-                f.ze = Z[s1];
+                f.dz = DZX[s1];
                 f.act = ACT[s2] & ACT[s1];
                 f.q0 = QX[s1];
                 f.u0 = U[s1];
@@ -518,8 +550,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
                 Face2 f;
                 f.hw = HL[s1];
                 f.he = H[s1];
-                f.zw = ZL[s1];
-                f.ze = Z[s1];
+                f.dz = DZY[s1];
                 f.act = ACTL[s1] & ACT[s1];
                 f.q0 = QY[s1];
                 f.u0 = V[s1];
@@ -672,6 +703,7 @@ __global__ void __launch_bounds__(NT, 4) k32_march(const Scn32* __restrict__ scn
         pr.sy = my * rdxy.y;
         part[w.w] = pr; /* the partials stay in scenario order whatever the launch order */
     }
+    return true;
 }
 
 /* ---------------- per-scenario finalize ---------------------------------- */
@@ -711,25 +743,27 @@ __device__ float source_at32(const Scn32& P, int i, double time) {
     return (float)(q / (P.dxd * P.dyd));
 }
 
-__device__ void prepare_slot32(const Scn32& P, Clock32* clk) {
-    const double t = clk->t;
+/* Length and forcing of the iteration starting at time t.  The clock is
+ * accessed as volatile: inside a persistent launch the CTA that reduces a
+ * scenario's iteration may sit on another SM than the previous one's. */
+__device__ void prepare_slot32(const Scn32& P, volatile Clock32* clk, double t, double t_end, double s_max) {
     double dt2, tm;
     int active;
     if (P.dt_mode == 0) {
         /* the reference's time grid: the clock advances by dt twice, as the
          * FP64 path's; only the state update uses dt2 rounded to binary32 */
         const double dt = P.dt_fixed;
-        active = (t + dt <= clk->t_end);
+        active = (t + dt <= t_end);
         dt2 = 2.0 * dt;
         tm = t + dt;
     } else {
-        active = (t < clk->t_end);
-        dt2 = clk->s_max > 0 ? fmin(P.dt_max, P.cfl / clk->s_max) : P.dt_max;
+        active = (t < t_end);
+        dt2 = s_max > 0 ? fmin(P.dt_max, P.cfl / s_max) : P.dt_max;
         dt2 = (double)(float)dt2;
-        if (t + dt2 > clk->t_end) dt2 = clk->t_end - t;
+        if (t + dt2 > t_end) dt2 = t_end - t;
         tm = t + 0.5 * dt2;
     }
-    Slot32& s = clk->slot;
+    volatile Slot32& s = clk->slot;
     s.active = active;
     s.dt2 = (float)dt2;
     s.dt2dx = (float)(dt2 / P.dxd);
@@ -750,24 +784,23 @@ __device__ void prepare_slot32(const Scn32& P, Clock32* clk) {
     if (!active) clk->done = 1;
 }
 
-/* one warp per scenario: fixed-order sum of its tile partials */
-__global__ void k32_finalize(const Scn32* __restrict__ scns, int nscn, const Part32* __restrict__ part) {
-    const int s = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+/* One scenario's end of iteration, run by one warp: fixed-order sum of its
+ * work items' partials (read past L1: other CTAs wrote them during this
+ * launch), ledger, clock, outlet record and the next slot. */
+__device__ __noinline__ void finalize_scn(const Scn32& P, const Part32* __restrict__ part) {
     const int lane = threadIdx.x & 31;
-    if (s >= nscn) return;
-    const Scn32& P = scns[s];
-    Clock32* clk = P.clk;
+    volatile Clock32* clk = P.clk;
     if (!clk->slot.active) return;
     double clamp = 0, qout = 0, rain = 0, evc = 0;
     float sx = 0.f, sy = 0.f;
     for (int k = lane; k < P.nwork; k += 32) {
-        const Part32& q = part[P.first_work + k];
-        clamp += q.clamp;
-        qout += q.qout;
-        rain += q.rain;
-        evc += q.evap;
-        sx = fmaxf(sx, q.sx);
-        sy = fmaxf(sy, q.sy);
+        const Part32* q = part + P.first_work + k;
+        clamp += __ldcg(&q->clamp);
+        qout += __ldcg(&q->qout);
+        rain += __ldcg(&q->rain);
+        evc += __ldcg(&q->evap);
+        sx = fmaxf(sx, __ldcg(&q->sx));
+        sy = fmaxf(sy, __ldcg(&q->sy));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -779,40 +812,142 @@ __global__ void k32_finalize(const Scn32* __restrict__ scns, int nscn, const Par
         sy = fmaxf(sy, __shfl_down_sync(0xffffffffu, sy, o));
     }
     if (lane != 0) return;
-    const Slot32 sl = clk->slot;
+    const float rr2 = clk->slot.rr2, ev2 = clk->slot.ev2;
+    const int cur = clk->slot.cur;
     const double dt2 = clk->dt2;
     const double area = P.area;
     const double rain_sum = P.ledger_cells ? rain : P.rain_static;
-    clk->rain_in += dt2 * (double)sl.rr2 * rain_sum * area;
-    clk->evap_out += dt2 * (double)sl.ev2 * evc * area;
+    clk->rain_in = clk->rain_in + dt2 * (double)rr2 * rain_sum * area;
+    clk->evap_out = clk->evap_out + dt2 * (double)ev2 * evc * area;
     double qsrc = 0.0;
     for (int k = 0; k < P.nsrc; k++) qsrc += (double)clk->ql2[k];
-    clk->source_in += dt2 * qsrc * area;
-    clk->clamp_gain += clamp * area;
-    clk->q_out = qout * P.dyd;
-    clk->outflow += dt2 * clk->q_out;
+    clk->source_in = clk->source_in + dt2 * qsrc * area;
+    clk->clamp_gain = clk->clamp_gain + clamp * area;
+    const double q_out = qout * P.dyd;
+    clk->q_out = q_out;
+    clk->outflow = clk->outflow + dt2 * q_out;
     /* the CFL speed of the state this iteration started from */
-    clk->s_max = (double)sx + (double)sy;
-    if (!isfinite(clk->s_max) || !isfinite(qout)) clk->status |= 1;
-    clk->t = (P.dt_mode == 0) ? (clk->t + P.dt_fixed) + P.dt_fixed : clk->t + dt2;
-    clk->iters += 1;
-    clk->slot.cur = sl.cur ^ 1;
+    const double s_max = (double)sx + (double)sy;
+    clk->s_max = s_max;
+    if (!isfinite(s_max) || !isfinite(qout)) clk->status = clk->status | 1;
+    const double t = (P.dt_mode == 0) ? (clk->t + P.dt_fixed) + P.dt_fixed : clk->t + dt2;
+    clk->t = t;
+    clk->iters = clk->iters + 1;
+    clk->slot.cur = cur ^ 1;
     if (P.outlet) {
         const long long k = clk->outlet_n % P.outlet_cap;
-        P.outlet[2 * k] = clk->t;
-        P.outlet[2 * k + 1] = clk->q_out;
-        clk->outlet_n += 1;
+        P.outlet[2 * k] = t;
+        P.outlet[2 * k + 1] = q_out;
+        clk->outlet_n = clk->outlet_n + 1;
     }
-    prepare_slot32(P, clk);
+    prepare_slot32(P, clk, t, clk->t_end, s_max);
+}
+
+/* ---------------- the persistent launch ---------------------------------- */
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+/* The queue side of the persistent loop, run by thread 0: the next ticket
+ * and the bounded wait for its scenario's previous iteration.  Returns the
+ * ticket, or ~0u when the CTA is to leave (the queue is empty, or a wait
+ * ran out: then the scenario's timeout bit and the abort flag are set). */
+__device__ __noinline__ unsigned fetch_ticket(const Scn32* __restrict__ scns, const int4* __restrict__ work, int nwork,
+                                              int niter, Ctl32* ctl) {
+    const int* done = reinterpret_cast<const int*>(ctl + 1);
+    volatile unsigned* abort_flag = &ctl->abort;
+    const unsigned q = atomicAdd(&ctl->next, 1u);
+    if (q >= (unsigned)nwork * (unsigned)niter || *abort_flag) return ~0u;
+    const int it = (int)(q / (unsigned)nwork);
+    const int sc = work[q % (unsigned)nwork].x;
+    const long long t0 = clock64();
+    while (ld_acquire_gpu(&done[sc]) < it) {
+        if (*abort_flag) return ~0u;
+        if (clock64() - t0 > (1ll << 31)) {
+            atomicOr(&scns[sc].clk->status, 2);
+            *abort_flag = 1u;
+            return ~0u;
+        }
+        __nanosleep(100);
+    }
+    return q;
+}
+
+/* thread 0 after an item of scenario sc: count it; true when it was the
+ * scenario's last of the iteration */
+__device__ __noinline__ bool count_item(const Scn32* __restrict__ scns, int nscn, int sc, Ctl32* ctl) {
+    unsigned* cnt = reinterpret_cast<unsigned*>(reinterpret_cast<int*>(ctl + 1) + nscn);
+    __threadfence(); /* the item's state and partial before its count */
+    return atomicAdd(&cnt[sc], 1u) == (unsigned)scns[sc].nwork - 1u;
+}
+
+/* thread 0 after the scenario's reduction: release its next iteration */
+__device__ __noinline__ void release_scenario(int nscn, int sc, int iterations_done, Ctl32* ctl) {
+    int* done = reinterpret_cast<int*>(ctl + 1);
+    unsigned* cnt = reinterpret_cast<unsigned*>(done + nscn);
+    cnt[sc] = 0u;
+    __threadfence();
+    st_release_gpu(&done[sc], iterations_done);
+}
+
+/* niter iterations of the scenarios of one feature class.  Every CTA takes
+ * queue tickets q = 0, 1, ...: ticket q is work item q % nwork of iteration
+ * q / nwork.  Before an item of iteration it starts, its scenario must have
+ * completed iteration it-1 in this launch (done[s] >= it).  The tickets a
+ * scenario waits for were all handed out earlier to CTAs that are running
+ * (the launch is cooperative: every CTA is resident), so the waits end; they
+ * are bounded all the same (about 2^31 cycles), after which the CTA sets the
+ * abort flag and the scenario's timeout bit, and every CTA leaves.  The CTA
+ * that finishes a scenario's last item of an iteration reduces the
+ * scenario's partials in a fixed order, advances its clock and releases
+ * done[s] = it + 1.  done and cnt follow the control block, nscn ints each. */
+template <bool CLS, bool RW, bool LAKE, bool SRC>
+__global__ void __launch_bounds__(NT, 4) k32_persist(const Scn32* __restrict__ scns, int nscn,
+                                                     const int4* __restrict__ work, int nwork, int niter,
+                                                     Part32* __restrict__ part, Ctl32* ctl) {
+    extern __shared__ unsigned char smem_raw[];
+    SmemM& S = *reinterpret_cast<SmemM*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    for (;;) {
+        if (threadIdx.x == 0) S.q = fetch_ticket(scns, work, nwork, niter, ctl);
+        __syncthreads();
+        /* read through a shuffle from lane 0: the compiler then knows the
+         * ticket, the item and the scenario's fields are uniform across the
+         * warp and keeps them in uniform registers, leaving the 128 per
+         * thread to the marching windows */
+        const unsigned q = __shfl_sync(0xffffffffu, S.q, 0);
+        if (q == ~0u) break;
+        const int4 w = work[q % (unsigned)nwork];
+        /* the previous iteration's state was written by other CTAs with
+         * generic stores; this item reads it with TMA (the async proxy) */
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+        if (!march_item<CLS, RW, LAKE, SRC>(S, scns[w.x], w, part)) {
+            if (threadIdx.x == 0) ctl->abort = 1u;
+            break;
+        }
+        if (threadIdx.x == 0) S.last = count_item(scns, nscn, w.x, ctl);
+        __syncthreads();
+        if (__shfl_sync(0xffffffffu, S.last, 0) && threadIdx.x < 32) {
+            __threadfence();
+            finalize_scn(scns[w.x], part);
+            if (threadIdx.x == 0) release_scenario(nscn, w.x, (int)(q / (unsigned)nwork) + 1, ctl);
+        }
+        __syncthreads();
+    }
 }
 
 /* first slot of every scenario from its clock (t, s_max, t_end) */
 __global__ void k32_prime(const Scn32* __restrict__ scns, int nscn) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nscn) return;
-    Clock32* clk = scns[s].clk;
+    volatile Clock32* clk = scns[s].clk;
     clk->done = 0;
-    prepare_slot32(scns[s], clk);
+    prepare_slot32(scns[s], clk, clk->t, clk->t_end, clk->s_max);
 }
 
 /* volume = sum of (h - kc) over active cells, and the CFL face speed of the
@@ -901,16 +1036,16 @@ __global__ void __launch_bounds__(1024) k32_volume_fin(const Scn32* __restrict__
 
 size_t fp32_volume_scratch_bytes() { return 32 + kVolBlocks * sizeof(VolPart); }
 
-typedef void (*MarchFn)(const Scn32*, const int4*, Part32*);
-static const MarchFn kMarch[T32_NCLASS] = {
-    k32_march<false, false, false, false>, k32_march<true, false, false, false>,
-    k32_march<false, true, false, false>,  k32_march<true, true, false, false>,
-    k32_march<false, false, true, false>,  k32_march<true, false, true, false>,
-    k32_march<false, true, true, false>,   k32_march<true, true, true, false>,
-    k32_march<false, false, false, true>,  k32_march<true, false, false, true>,
-    k32_march<false, true, false, true>,   k32_march<true, true, false, true>,
-    k32_march<false, false, true, true>,   k32_march<true, false, true, true>,
-    k32_march<false, true, true, true>,    k32_march<true, true, true, true>,
+typedef void (*PersistFn)(const Scn32*, int, const int4*, int, int, Part32*, Ctl32*);
+static const PersistFn kPersist[T32_NCLASS] = {
+    k32_persist<false, false, false, false>, k32_persist<true, false, false, false>,
+    k32_persist<false, true, false, false>,  k32_persist<true, true, false, false>,
+    k32_persist<false, false, true, false>,  k32_persist<true, false, true, false>,
+    k32_persist<false, true, true, false>,   k32_persist<true, true, true, false>,
+    k32_persist<false, false, false, true>,  k32_persist<true, false, false, true>,
+    k32_persist<false, true, false, true>,   k32_persist<true, true, false, true>,
+    k32_persist<false, false, true, true>,   k32_persist<true, false, true, true>,
+    k32_persist<false, true, true, true>,    k32_persist<true, true, true, true>,
 };
 
 int fp32_feature_class(const Scn32& d) {
@@ -919,20 +1054,42 @@ int fp32_feature_class(const Scn32& d) {
 
 int fp32_configure_kernels() {
     for (int k = 0; k < T32_NCLASS; k++) {
-        cudaError_t e = cudaFuncSetAttribute(kMarch[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(kPersist[k], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)fp32_smem_bytes_variant(k));
         if (e != cudaSuccess) return -1;
     }
     return 0;
 }
 
-void fp32_launch_iteration(const Scn32* d_scn, int nscn, const int4* d_work, const int* class_first,
-                           const int* class_n, Part32* d_part, cudaStream_t s) {
-    for (int k = 0; k < T32_NCLASS; k++)
-        if (class_n[k] > 0)
-            kMarch[k]<<<class_n[k], NT, fp32_smem_bytes_variant(k), s>>>(d_scn, d_work + class_first[k],
-                                                                d_part + class_first[k]);
-    k32_finalize<<<(nscn + 3) / 4, 128, 0, s>>>(d_scn, nscn, d_part);
+int fp32_blocks_per_sm(int k) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kPersist[k], NT, fp32_smem_bytes_variant(k)) != cudaSuccess)
+        return 0;
+    return n;
+}
+
+cudaError_t fp32_launch_chunk(const Scn32* d_scn, int nscn, const int4* d_work, const int* class_first,
+                              const int* class_n, Part32* d_part, void* d_ctl, int niter, const int* grid,
+                              cudaStream_t s) {
+    for (int k = 0; k < T32_NCLASS; k++) {
+        if (class_n[k] <= 0) continue;
+        cudaError_t e = cudaMemsetAsync(d_ctl, 0, fp32_ctl_bytes(nscn), s);
+        if (e != cudaSuccess) return e;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid[k]);
+        cfg.blockDim = dim3(NT);
+        cfg.dynamicSmemBytes = fp32_smem_bytes_variant(k);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative; /* every CTA resident: the dataflow waits end */
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, kPersist[k], d_scn, nscn, d_work + class_first[k], class_n[k], niter, d_part,
+                               static_cast<Ctl32*>(d_ctl));
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 void fp32_launch_prime(const Scn32* d_scn, int nscn, cudaStream_t s) {

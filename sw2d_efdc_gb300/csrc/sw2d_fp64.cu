@@ -16,7 +16,11 @@
  *                outlet sums by block reduction; the last block reduces the
  *                per-block partials in a fixed order and prepares the next
  *                iteration's length and forcing on the device.
- * forward (:670-693) is a buffer swap.
+ * forward (:670-693) is a buffer swap for the depth (h[cur] -> h[nxt]); the
+ * discharges keep fixed roles: qx[0]/qy[0] hold the state, k64_flux writes
+ * its new faces into qx[1]/qy[1], and k64_update writes every face, closed
+ * or not, back into qx[0]/qy[0] -- so no tile reads a face another tile has
+ * already closed (the provisional depth needs them unclosed).
  * Compiled with --fmad=false: every expression is evaluated with the same
  * roundings as the CPU oracle (gcc -ffp-contract=off), explicit fma() only
  * where sw2d_math.h spells it.
@@ -256,14 +260,13 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int c = blockIdx.x * SW2D_BX + tx;
     const int r = blockIdx.y * SW2D_BY + ty;
-    const int nxt = cur ^ 1;
     const Slot& s = p.clk->slot[cur];
     const bool in = (r <= p.R && c <= p.C);
     const int P = p.P;
     const size_t i = (size_t)(r + H) * P + (c + H);
     const double* __restrict__ h = p.h[cur];
-    const double* __restrict__ umo = p.qx[cur];
-    const double* __restrict__ vno = p.qy[cur];
+    const double* __restrict__ umo = p.qx[0]; /* the state's discharges */
+    const double* __restrict__ vno = p.qy[0];
     const double* __restrict__ uu1 = p.uu1;
     const double* __restrict__ vv1 = p.vv1;
     const double th = p.th;
@@ -307,10 +310,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
     bool okx = false, oky = false;
     double hmx = 0, hmy = 0, vx = 0, vy = 0;
     if (in) {
-        if (!s.active) {
-            if (c < p.C) p.qx[nxt][i] = umo[i];
-            if (r < p.R) p.qy[nxt][i] = vno[i];
-        } else {
+        if (s.active) {
             const double dt2 = s.dt2, dt2dx = s.dt2dx, dt2dy = s.dt2dy, gg = p.g;
             /* mean depths of the two faces: the momentum update and the CFL speed */
             const double hmX = (doX && r > 0) ? sw2d_half(h[i] + h[i - P]) : 0.0;
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
                 } else {
                     F = face_special(fx, th, gg);
                 }
-                p.qx[nxt][i] = F;
+                p.qx[1][i] = F;
             }
             if (doY) {
                 double F;
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
                 } else {
                     F = face_special(fy, th, gg);
                 }
-                p.qy[nxt][i] = F;
+                p.qy[1][i] = F;
             }
             if (p.dt_mode == 1) {
                 const uint8_t fc = p.flags[i];
@@ -480,7 +480,6 @@ __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
     if (!last) return;
     __threadfence();
     double vr = 0.0, ve = 0.0, vq = 0.0;
-    unsigned long long vs = 0ull;
     for (int b = tid; b < nblocks; b += SW2D_BX * SW2D_BY) {
         const volatile double* pb = p.partials + (size_t)b * NPART;
         vr += pb[0];
@@ -505,7 +504,6 @@ __device__ void finish_iteration(const StepParams& p, int cur, int nblocks) {
         ux = block_max_u64(ux, smu);
         uy = block_max_u64(uy, smu);
     }
-    (void)vs;
     if (tid == 0) {
         DevClock* clk = p.clk;
         const Slot& s = clk->slot[cur];
@@ -569,8 +567,8 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_update(StepParams p, in
     const Slot& s = p.clk->slot[cur];
     const int P = p.P, R = p.R, C = p.C;
     const double th = p.th;
-    const double* __restrict__ fx = p.qx[nxt];
-    const double* __restrict__ fy = p.qy[nxt];
+    const double* __restrict__ fx = p.qx[1]; /* k64_flux's new discharges, read only */
+    const double* __restrict__ fy = p.qy[1];
     const double* __restrict__ hc = p.h[cur];
     double vr = 0.0, ve = 0.0, vq = 0.0;
     if (!s.active) {
@@ -647,10 +645,8 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_update(StepParams p, in
             const int dr = rr + 2, dc = cc + 2, nr = rr + 1, nc = cc + 1;
             if (c < C) {
                 double F = fx[i];
-                if ((sw2d_gt0(F) && sdry[dr - 1][dc]) || (sw2d_lt0(F) && sdry[dr][dc])) {
-                    F = 0;
-                    p.qx[nxt][i] = F;
-                }
+                if ((sw2d_gt0(F) && sdry[dr - 1][dc]) || (sw2d_lt0(F) && sdry[dr][dc])) F = 0;
+                p.qx[0][i] = F;
                 double hm;
                 if (r == 0) hm = shn[nr][nc];
                 else if (r == R) hm = shn[nr - 1][nc];
@@ -659,10 +655,8 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_update(StepParams p, in
             }
             if (r < R) {
                 double F = fy[i];
-                if ((sw2d_gt0(F) && sdry[dr][dc - 1]) || (sw2d_lt0(F) && sdry[dr][dc])) {
-                    F = 0;
-                    p.qy[nxt][i] = F;
-                }
+                if ((sw2d_gt0(F) && sdry[dr][dc - 1]) || (sw2d_lt0(F) && sdry[dr][dc])) F = 0;
+                p.qy[0][i] = F;
                 double hn;
                 if (c == 0) hn = shn[nr][nc];
                 else if (c == C) hn = shn[nr][nc - 1];
@@ -779,7 +773,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, i
     const double* __restrict__ h = p.h[cur];
     const double th = p.th;
     if (c < p.C) {
-        const double F = p.qx[cur][i];
+        const double F = p.qx[0][i];
         double hm;
         if (r == 0) hm = h[i];
         else if (r == p.R) hm = h[i - P];
@@ -787,7 +781,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, i
         p.uu1[i] = sw2d_ge_pos(hm, th) ? (sw2d_is0(F) ? F : F / hm) : 0.00; /* 0/hm is 0 of F's sign */
     }
     if (r < p.R) {
-        const double F = p.qy[cur][i];
+        const double F = p.qy[0][i];
         double hn;
         if (c == 0) hn = h[i];
         else if (c == p.C) hn = h[i - 1];

@@ -40,7 +40,7 @@ def test_python_mirror_covers_the_header():
 def test_config_default_and_abi_version():
     cfg = api.default_config()
     assert cfg.th == 1e-4 and cfg.g == 9.80 and cfg.dt == 0.04
-    assert api.load().sw2d_abi_version() == 1
+    assert api.load().sw2d_abi_version() == 2
 
 
 def test_create_rejects_bad_config_without_touching_the_gpu():
@@ -70,7 +70,7 @@ C_PROGRAM = r"""
 int main(void) {
     sw2d_config cfg;
     sw2d_handle* h = NULL;
-    if (sw2d_abi_version() != 1) return 10;
+    if (sw2d_abi_version() != 2) return 10;
     if (sw2d_config_default(&cfg) != SW2D_OK || cfg.rows != 0 || cfg.g != 9.80) return 11;
     cfg.rows = 1; cfg.cols = 8;
     if (sw2d_create(&cfg, &h) != SW2D_ERR_INVALID || h != NULL) return 12;

@@ -118,10 +118,11 @@ def test_cancel_mid_run_frees_the_slot_and_leaves_the_others_unchanged():
     bt.close()
 
 
-def test_rows_per_item_setting():
-    """A batch of scenarios that arrive together may use longer work items;
-    results then stay the same alone and in the mix, and differ from the
-    default tiling (other tile datums) within the FP32 form's 1 mm."""
+def test_rows_per_item_does_not_change_results():
+    """The rows per work item (the autotuner's knob) change only the work
+    split: the bed's datum tiles are fixed at 224 x 64 cells, so every
+    setting, and the tuned default, gives bit-identical results, alone and
+    in a mix."""
     a = scenario(300, 31, 60.0)
 
     def run(specs, rows):
@@ -130,16 +131,52 @@ def test_rows_per_item_setting():
         ids = [b.submit(**s) for s in specs]
         while b.step(32) != (0, 0):
             pass
-        out = b.result(ids[-1])[0]
+        out = b.result(ids[-1])
+        st = b.stats()
         b.close()
-        return out
+        return out, st
 
-    alone = run([a], 256)
-    mixed = run([scenario(500, 32, 30.0), scenario(140, 33, 90.0), a], 256)
-    assert np.array_equal(alone, mixed)
-    default = run([a], 0)
-    assert np.abs(alone - default).max() < 1e-3  # the FP32 form's depth tolerance
+    ref, st = run([a], 256)
+    assert st["rows_per_item"] == 256
+    for rows, specs in ((64, [a]), (128, [scenario(500, 32, 30.0), scenario(140, 33, 90.0), a]), (512, [a]),
+                        (0, [scenario(1200, 34, 20.0), a])):
+        got, _ = run(specs, rows)
+        assert all(np.array_equal(x, y) for x, y in zip(ref, got)), rows
     b = api.Batch()
     with pytest.raises(api.Sw2dError):
         b.set_rows_per_item(30)
+    with pytest.raises(api.Sw2dError):
+        b.set_rows_per_item(1024)
+    b.close()
+
+
+def test_request_submitted_while_others_run_matches_alone():
+    """Continuous batching: a request that arrives while other requests are
+    already advancing on the GPU joins at the next step and finishes
+    bit-identical to the same request run alone; the requests that were
+    running are unchanged by its arrival."""
+    late = scenario(170, 41, 70.0)
+    early = [scenario(240, 42, 90.0), scenario(120, 43, 50.0)]
+    alone_late = run_batch([late])[0][0]
+    alone_early = [run_batch([s])[0][0] for s in early]
+    b = api.Batch()
+    ids = [b.submit(**s) for s in early]
+    nr, nq = b.step(24)
+    assert nr == 2 and nq == 0
+    assert all(b.poll(i)[0] == api.REQ_RUNNING for i in ids)
+    t_before = [b.poll(i)[1]["time"] for i in ids]
+    assert all(0.0 < t < 50.0 for t in t_before)  # mid-run
+    il = b.submit(**late)
+    nr, nq = b.step(8)
+    assert nr == 3 and b.poll(il)[0] == api.REQ_RUNNING
+    for _ in range(10000):
+        nr, nq = b.step(32)
+        if nr == 0 and nq == 0:
+            break
+    for i, (res, led) in zip(ids + [il], alone_early + [alone_late]):
+        st, l1 = b.poll(i)
+        assert st == api.REQ_DONE
+        got = b.result(i)
+        assert all(np.array_equal(x, y) for x, y in zip(got, res))
+        assert l1["time"] == led["time"] and l1["iterations"] == led["iterations"]
     b.close()

@@ -150,6 +150,27 @@ def test_step_counts_and_odd_steps():
     _assert_same(_fields(m), od.fields())
 
 
+@pytest.mark.parametrize("dt_mode", [O.DT_FIXED, O.DT_CFL])
+def test_many_tiles_bitwise(dt_mode):
+    """A raster of several update tiles in both directions (tiles of 64 x 16
+    cells; NODATA holes on tile edges), so that every tile edge, the halo of
+    recomputed provisional and final depths and the face write-back are
+    exercised, bit for bit against the oracle."""
+    rng = np.random.default_rng(12)
+    case = bumpy_case(R=150, C=210, seed=13, dt_mode=dt_mode, cfl=0.7, dt_max=1.0, outflow_south=True,
+                      rain_mode=O.RAIN_STEP, rain=np.array([40.0, 10.0, 0.0, 25.0]), dtrain=20.0, t_end=70.0)
+    case.dem[15:18, 60:70] = -9999.0
+    case.dem[40:50, 127:130] = -9999.0
+    case.h0[case.dem == -9999.0] = 0.0
+    case.h0[60:100, 100:180] = 0.25 * rng.random((40, 80))
+    case.manning_field = rng.choice([0.02, 0.05, 0.10], size=case.dem.shape)
+    m, od, ol, n = _run_pair(case)
+    assert n == od.iters > 50
+    _assert_same(_fields(m), od.fields())
+    assert np.abs(m.depth() - ol.fields()["h"]).max() <= DH_TOL
+    m.close()
+
+
 def test_cfl_odd_step_counts():
     """CFL mode takes any iteration count: an odd bounded count ends with an
     inactive iteration the device's iteration limit sets up."""
