@@ -273,10 +273,16 @@ __device__ __forceinline__ Slot32 load_slot(const Clock32* clk) {
 static_assert(sizeof(Slot32) % 16 == 0 && offsetof(Clock32, slot) == 0, "slot read as int4");
 
 /* One work item: a strip of one scenario over `seg` rows, one iteration.
- * Returns false when a staged load did not arrive in time (the status bit
- * is set; the launch's results are void). */
+ * gb counts the staged blocks the CTA has used so far: block b of this item
+ * goes to stage (gb + b) % NS and completes that stage's barrier phase
+ * (gb + b) / NS, so the barriers, initialised once per CTA, keep their
+ * phases from item to item (an mbarrier is never re-initialised while the
+ * copy engine may still hold state for it).  Returns false when a staged
+ * load did not arrive in time (the status bit is set; the launch's results
+ * are void). */
 template <bool CLS, bool RW, bool LAKE, bool SRC>
-__device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 w, Part32* __restrict__ part) {
+__device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 w, Part32* __restrict__ part,
+                                           unsigned& gb) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     Clock32* clk = P.clk;
     const Slot32 sl = load_slot(clk);
@@ -302,12 +308,6 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
             part[w.w] = zp;
         }
         return true; /* tile skipped, status bit 2 */
-    }
-    if (tid == 0) {
-        /* every load of the previous item was waited for: the barriers are
-         * idle and start again at phase 0 */
-        for (int k = 0; k < NS; k++) mbar_init(&S.bar[k], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (tid < T32_MAXCLASS) S.ntab[tid] = P.ntab[tid];
     if (SRC && warp == 0) {
@@ -366,7 +366,7 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
     if (tid == 0 && !P.stall_staging) {
         /* the staging buffers were last read by the generic proxy */
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (int b = 0; b < NS && b < nblk; b++) issue(b, b);
+        for (int b = 0; b < NS && b < nblk; b++) issue(b, (int)((gb + b) % NS));
     }
 
     /* lane geometry: staged columns sc, sc+1; global columns cg, cg+1 */
@@ -422,11 +422,11 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
     };
 
     for (int b = 0; b < nblk; b++) {
-        const int st = b % NS;
+        const int st = (int)((gb + b) % NS);
         /* bounded wait for the block (about 2^31 cycles); the CTA agrees on
          * the outcome so that no warp is left waiting at a barrier */
         {
-            const unsigned par = (unsigned)((b / NS) & 1);
+            const unsigned par = ((gb + b) / NS) & 1u;
             long long t0 = clock64();
             bool ok = true;
             while (!mbar_try_wait(&S.bar[st], par)) {
@@ -447,7 +447,7 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
                     const int issued = P.stall_staging ? 0 : min(nblk, b + NS);
                     for (int bb = b; bb < issued; bb++) {
                         const long long t1 = clock64();
-                        while (!mbar_try_wait(&S.bar[bb % NS], (unsigned)((bb / NS) & 1)) &&
+                        while (!mbar_try_wait(&S.bar[(gb + bb) % NS], ((gb + bb) / NS) & 1u) &&
                                clock64() - t1 <= (1ll << 31)) {
                         }
                     }
@@ -668,6 +668,7 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
             issue(b + NS, st);
         }
     }
+    gb += (unsigned)nblk;
 
     /* block reductions: warp sums in binary32, across warps in binary64 */
 #pragma unroll
@@ -911,8 +912,16 @@ template <bool CLS, bool RW, bool LAKE, bool SRC>
 __global__ void __launch_bounds__(NT, 4) k32_persist(const Scn32* __restrict__ scns, int nscn,
                                                      const int4* __restrict__ work, int nwork, int niter,
                                                      Part32* __restrict__ part, Ctl32* ctl) {
-    extern __shared__ unsigned char smem_raw[];
-    SmemM& S = *reinterpret_cast<SmemM*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    /* aligned by a byte offset from the shared array itself, so that the
+     * compiler keeps the shared address space (shared loads, not generic) */
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    SmemM& S = *reinterpret_cast<SmemM*>(smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u));
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < NS; k++) mbar_init(&S.bar[k], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    unsigned gb = 0; /* staged blocks used so far by this CTA */
     for (;;) {
         if (threadIdx.x == 0) S.q = fetch_ticket(scns, work, nwork, niter, ctl);
         __syncthreads();
@@ -926,7 +935,7 @@ __global__ void __launch_bounds__(NT, 4) k32_persist(const Scn32* __restrict__ s
         /* the previous iteration's state was written by other CTAs with
          * generic stores; this item reads it with TMA (the async proxy) */
         asm volatile("fence.proxy.async.global;" ::: "memory");
-        if (!march_item<CLS, RW, LAKE, SRC>(S, scns[w.x], w, part)) {
+        if (!march_item<CLS, RW, LAKE, SRC>(S, scns[w.x], w, part, gb)) {
             if (threadIdx.x == 0) ctl->abort = 1u;
             break;
         }
