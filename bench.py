@@ -41,7 +41,7 @@ BYTES_PER_CELL_K64_FLUX = 66
 # dram__bytes_read.sum + dram__bytes_write.sum = 821.7 + 251.0 MB over 16.78 M cells
 TRAFFIC_PER_CELL_K64_FLUX = 63.93
 BYTES_PER_CELL_FP32_CFG3 = 37  # h,qx,qy r+w 24 + z offset 4 + info byte 1 + Kahan compensation r+w 8
-# DRAM bytes per cell of one k32_march launch, 4096 x 4096 precision form at t = 1200 s: ncu
+# DRAM bytes per cell-update of the FP32 step (k32_march, the per-iteration kernel before the persistent one), 4096 x 4096 precision form at t = 1200 s: ncu
 # dram__bytes_read.sum + dram__bytes_write.sum = 360.3 + 221.8 MB over 16.78 M cells; the
 # launch streams every field once, so the figure scales with cells
 TRAFFIC_PER_CELL_K32_MARCH = 34.69
@@ -276,7 +276,7 @@ def run_fp32_leg(args, peak):
         "workload": "FP32 precision form %dx%d dx=1m tilted plane + bumps, gamma 5-min hyetograph "
                     "(shape 0.8, mean 20 mm/h), CFL 0.7, free south outlet, timed from t=%.0f s"
                     % (sc.rows, sc.cols, t_spun),
-        "roofline": {"bound": "hbm", "kernel": "k32_march + k32_finalize",
+        "roofline": {"bound": "hbm", "kernel": "k32_persist",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3,
                      "traffic": round(TRAFFIC_PER_CELL_K32_MARCH * cells / 1e9, 4),
@@ -503,7 +503,6 @@ def run_batched_leg(args, peak, fp64_value):
     specs = make_batch_specs(args.batch_n, 128, 2048, 4)
     gen_s = time.time() - t0
     b = api.Batch(device=device())
-    b.set_rows_per_item(256)  # the scenarios arrive together: fewer halo rows beat more work items
     for sp in specs:
         b.submit(**sp)
     b.step(0)
@@ -520,11 +519,14 @@ def run_batched_leg(args, peak, fp64_value):
     achieved = value * (BYTES_PER_CELL_FP32_CFG3 + 1)  # + the class byte
     return {"value": round(value, 4), "unit": UNIT, "scenarios": len(specs), "cells": int(cells),
             "steps": args.steps, "ms_per_step": round(ms / args.steps, 4),
+            "rows_per_item": st1["rows_per_item"], "tuning_ms": round(st1["tuning_ms"], 1),
+            "launches": int(st1["launches"] - st0["launches"]),
             "workload": "batched FP32: %d scenarios, side log-uniform 128-2048, fractal DEM, 3-class Voronoi n, "
-                        "gamma hyetographs, per-scenario CFL length, one row-marching launch per iteration "
-                        "(every scenario has a class raster: one feature class) and a finalize, "
-                        "256 rows per work item" % len(specs),
-            "roofline": {"bound": "hbm", "kernel": "k32_march + k32_finalize", "achieved": round(achieved, 2),
+                        "gamma hyetographs, per-scenario CFL length; one persistent cooperative launch per chunk "
+                        "of up to 32 iterations (every scenario has a class raster: one feature class), each "
+                        "scenario's iterations chained on the device; rows per work item chosen by the "
+                        "autotuner (%d)" % (len(specs), st1["rows_per_item"]),
+            "roofline": {"bound": "hbm", "kernel": "k32_persist", "achieved": round(achieved, 2),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3 + 1},
             "vs_fp64_plain": round(value / fp64_value, 3) if fp64_value else None,
@@ -582,6 +584,7 @@ def run_served_leg(args, fp64_value):
             "value": round(stats["cell_updates"] / (stats["device_ms"] * 1e-3) / 1e9, 4), "unit": UNIT,
             "vs_fp64_plain": round(stats["cell_updates"] / (stats["device_ms"] * 1e-3) / 1e9 / fp64_value, 3)
             if fp64_value else None,
+            "tuning_s": round(stats["tuning_ms"] / 1e3, 3), "rows_per_item": stats["rows_per_item"],
             "workload": "served FP32: Poisson arrivals 20/s, side log-uniform 256-4096, durations U(1,6) h x %g, "
                         "HBM budget 150 GB, continuous admission" % args.serve_time_scale,
             "input_generation_s": round(gen_s, 1)}
@@ -841,7 +844,7 @@ def main():
                     help="bracket the timed regions with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--no-prec", action="store_true", help="skip the precision-form error report")
     ap.add_argument("--no-config1", action="store_true", help="skip the 256x256 whole-run line")
-    ap.add_argument("--prec-size", type=int, default=2048)
+    ap.add_argument("--prec-size", type=int, default=1024)
     ap.add_argument("--prec-t", type=float, default=3 * 3600.0,
                     help="simulated seconds of the precision report (the generator's 3 h storm)")
     ap.add_argument("--prec-ensemble", action="store_true",
