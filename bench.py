@@ -455,8 +455,8 @@ def run_precision_leg(args):
                ("fp64_rain_plus_1e-6", api.FP64, 1.0 + 1e-6, 0.0, 0), ("fp64_bed_1e-7", api.FP64, 1.0, 1e-7, 17),
                ("fp64_rain_minus_1e-6", api.FP64, 1.0 - 1e-6, 0.0, 0)]
     if args.prec_ensemble:
-        members += [("fp64_bed_1e-7_b", api.FP64, 1.0, 1e-7, 18), ("fp64_rain_plus_3e-7", api.FP64, 1.0 + 3e-7, 0.0, 0),
-                    ("fp64_bed_1e-7_c", api.FP64, 1.0, 1e-7, 19)]
+        members += [("fp64_rain_plus_1e-5", api.FP64, 1.0 + 1e-5, 0.0, 0),
+                    ("fp64_rain_minus_1e-5", api.FP64, 1.0 - 1e-5, 0.0, 0), ("fp64_bed_1e-6", api.FP64, 1.0, 1e-6, 18)]
     size, T, dts = args.prec_size, args.prec_t, args.prec_sample
     sc, res = precision_runs(size, T, dts, members, dev=device())
     a = res["fp64"]

@@ -91,7 +91,6 @@ struct sw2d_handle {
     /* coupling */
     int nfaces = 0, lagged = 1;
     std::vector<int> f_side, f_i, f_j, f_cell;
-    std::vector<double> f_prev; /* FP32 handles: the previous sample's face velocities */
     void* pin = nullptr;        /* pinned staging of large device-to-host copies */
     size_t pin_bytes = 0;
     int* d_face = nullptr;      /* nfaces * 2: padded cell index, side */
@@ -1400,19 +1399,15 @@ int sw2d_set_coupling_mask(sw2d_handle* h, const int* mask, int lagged, int* n_f
     scan_coupling_faces(h->R, h->C, mask, &h->f_side, &h->f_i, &h->f_j, &h->f_cell);
     h->nfaces = (int)h->f_side.size();
     h->lagged = lagged ? 1 : 0;
-    if (h->fp32()) {
-        /* FP32 handles sample on the host from the downloaded state */
-        h->f_prev.assign((size_t)h->nfaces, 0.0);
-        if (n_faces_out) *n_faces_out = h->nfaces;
-        return SW2D_OK;
-    }
     dfree(h->d_face);
     dfree(h->d_face_vel);
     dfree(h->d_face_q);
+    /* the faces on the device: the FP64 kernel takes padded cell indices,
+     * the FP32 kernel raster indices (its scenario has its own pitch) */
     std::vector<int> dev((size_t)h->nfaces * 2 + 2);
     for (int k = 0; k < h->nfaces; k++) {
         int p = h->f_cell[k];
-        dev[2 * k] = (int)h->pad_index(p / cols, p % cols);
+        dev[2 * k] = h->fp32() ? p : (int)h->pad_index(p / cols, p % cols);
         dev[2 * k + 1] = h->f_side[k];
     }
     if ((rc = dalloc(&h->d_face, dev.size()))) return rc;
@@ -1443,29 +1438,17 @@ void launch_couple(const StepParams& p, int nfaces, const int* faces, int lagged
 }
 
 /* Boundary-discharge sample of an FP32 handle: the k_couple rule on the
- * host, from the state and its uua / vva (velocities_fp32). */
+ * scenario's device state (k32_couple), on the engine's stream. */
 static int couple_sample_fp32(sw2d_handle* h, int initial, double* q_out, int capacity) {
-    const size_t n = (size_t)h->R * h->C;
-    std::vector<double> d(n), uua(n), vva(n);
-    std::string err;
-    int rc = h->eng->get_state(h->eng_idx, d.data(), nullptr, nullptr, &err);
-    if (rc) return fail(rc, err);
-    if ((rc = velocities_fp32(h, nullptr, nullptr, uua.data(), vva.data()))) return rc;
-    const double dx = h->cfg.dx, dy = h->cfg.dy;
-    for (int k = 0; k < h->nfaces; k++) {
-        const int p = h->f_cell[k], side = h->f_side[k];
-        const double vnow = side <= 1 ? uua[p] : vva[p];
-        const double v = initial ? 0.0 : (h->lagged ? h->f_prev[k] : vnow);
-        const double hh = d[p];
-        double q;
-        switch (side) {
-        case 1: q = (v < 0) ? -v * hh * dx : 0.00; break; /* south */
-        case 0: q = (v > 0) ? v * hh * dx : 0.00; break;  /* north */
-        case 2: q = (v < 0) ? -v * hh * dy : 0.00; break; /* east */
-        default: q = (v > 0) ? v * hh * dy : 0.00; break; /* west */
-        }
-        if (q_out && k < capacity) q_out[k] = q;
-        h->f_prev[k] = vnow;
+    const sw2d::Scn32* d = h->eng->device_scenario(h->eng_idx);
+    if (!d) return fail(SW2D_ERR_CUDA, "FP32 scenario descriptor");
+    cudaStream_t st = h->eng->stream();
+    sw2d::fp32_launch_couple(d, h->nfaces, h->d_face, h->lagged, initial, h->cfg.th, h->d_face_vel, h->d_face_q, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    if (q_out) {
+        int n = std::min(capacity, h->nfaces);
+        CK(cudaMemcpy(q_out, h->d_face_q, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
     }
     return SW2D_OK;
 }

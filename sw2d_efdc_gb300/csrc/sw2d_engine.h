@@ -92,6 +92,11 @@ class Engine32 {
     int snapshot(int index, void* buf, std::string* err);
     int restore(int index, const void* buf, std::string* err);
     cudaStream_t stream() const { return stream_; }
+    /* the device descriptor of scenario i (valid after the work list is built) */
+    const Scn32* device_scenario(int i) {
+        std::string e;
+        return rebuild(&e) == SW2D_OK ? d_scn_ + i : nullptr;
+    }
     size_t bytes_in_use() const;
     double last_ms() const { return last_ms_; }
     long long last_iters() const { return last_iters_; }

@@ -1043,6 +1043,68 @@ __global__ void __launch_bounds__(1024) k32_volume_fin(const Scn32* __restrict__
     }
 }
 
+/* Boundary-discharge sample of an FP32 scenario (couple_BC_efdc,
+ * SW2D-EFDC.cu:728-1067, with the argument swap of its call at :4909): one
+ * thread per face (raster cell r * C + c, side 0 north / 1 south / 2 east /
+ * 3 west), the cross-face velocity uua (north, south) or vva (east, west) of
+ * the cell from the current state widened to binary64, inflow to the lake
+ * only; the FP64 path's k_couple rule on the FP32 state. */
+__device__ __forceinline__ double face_u32(const Scn32& P, const float* h, const float* q, int r, int c, double th) {
+    const size_t i = (size_t)(r + M_H) * P.P + (c + M_H);
+    double hm;
+    if (r == 0) hm = (double)h[i];
+    else if (r == P.R) hm = (double)h[i - P.P];
+    else hm = 0.5 * ((double)h[i] + (double)h[i - P.P]);
+    return hm >= th ? (double)q[i] / hm : 0.0;
+}
+__device__ __forceinline__ double face_v32(const Scn32& P, const float* h, const float* q, int r, int c, double th) {
+    const size_t i = (size_t)(r + M_H) * P.P + (c + M_H);
+    double hn;
+    if (c == 0) hn = (double)h[i];
+    else if (c == P.C) hn = (double)h[i - 1];
+    else hn = 0.5 * ((double)h[i] + (double)h[i - 1]);
+    return hn >= th ? (double)q[i] / hn : 0.0;
+}
+
+__global__ void k32_couple(const Scn32* __restrict__ scn, int nfaces, const int* __restrict__ faces, int lagged,
+                           int initial, double th, double* __restrict__ vel_prev, double* __restrict__ qout) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nfaces) return;
+    const Scn32& P = *scn;
+    const int cur = P.clk->slot.cur;
+    const float* h = P.h[cur];
+    const float* qx = P.qx[cur];
+    const float* qy = P.qy[cur];
+    const int cell = faces[2 * k], side = faces[2 * k + 1];
+    const int r = cell / P.C, c = cell - r * P.C;
+    double vnow;
+    if (side <= 1)
+        vnow = (c > 0) ? 0.250 * (face_u32(P, h, qx, r, c, th) + face_u32(P, h, qx, r + 1, c, th) +
+                                  face_u32(P, h, qx, r, c - 1, th) + face_u32(P, h, qx, r + 1, c - 1, th))
+                       : 0.50 * (face_u32(P, h, qx, r, c, th) + face_u32(P, h, qx, r + 1, c, th));
+    else
+        vnow = (r > 0) ? 0.250 * (face_v32(P, h, qy, r, c, th) + face_v32(P, h, qy, r, c + 1, th) +
+                                  face_v32(P, h, qy, r - 1, c, th) + face_v32(P, h, qy, r - 1, c + 1, th))
+                       : 0.50 * (face_v32(P, h, qy, r, c, th) + face_v32(P, h, qy, r, c + 1, th));
+    const double v = initial ? 0.0 : (lagged ? vel_prev[k] : vnow);
+    const double hh = (double)h[(size_t)(r + M_H) * P.P + (c + M_H)];
+    double out;
+    switch (side) {
+    case 1: out = (v < 0) ? -v * hh * P.dxd : 0.00; break; /* south */
+    case 0: out = (v > 0) ? v * hh * P.dxd : 0.00; break;  /* north */
+    case 2: out = (v < 0) ? -v * hh * P.dyd : 0.00; break; /* east */
+    default: out = (v > 0) ? v * hh * P.dyd : 0.00; break; /* west */
+    }
+    qout[k] = out;
+    vel_prev[k] = vnow;
+}
+
+void fp32_launch_couple(const Scn32* d_scn_one, int nfaces, const int* faces, int lagged, int initial, double th,
+                        double* vel_prev, double* q, cudaStream_t s) {
+    if (nfaces > 0)
+        k32_couple<<<(nfaces + 127) / 128, 128, 0, s>>>(d_scn_one, nfaces, faces, lagged, initial, th, vel_prev, q);
+}
+
 size_t fp32_volume_scratch_bytes() { return 32 + kVolBlocks * sizeof(VolPart); }
 
 typedef void (*PersistFn)(const Scn32*, int, const int4*, int, int, Part32*, Ctl32*);

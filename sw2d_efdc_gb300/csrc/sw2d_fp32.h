@@ -142,6 +142,11 @@ void fp32_launch_prime(const Scn32* d_scn, int nscn, cudaStream_t s);
  * fp32_volume_scratch_bytes() (the partials follow the two results) */
 void fp32_launch_volume(const Scn32* d_scn, int iscn, const Scn32& host_scn, double* d_out, cudaStream_t s);
 size_t fp32_volume_scratch_bytes();
+/* boundary-discharge sample of one scenario (device descriptor d_scn_one):
+ * faces holds (raster cell r*cols+c, side) pairs; q and vel_prev nfaces
+ * doubles on the device */
+void fp32_launch_couple(const Scn32* d_scn_one, int nfaces, const int* faces, int lagged, int initial, double th,
+                        double* vel_prev, double* q, cudaStream_t s);
 size_t fp32_smem_bytes();
 int fp32_configure_kernels();
 

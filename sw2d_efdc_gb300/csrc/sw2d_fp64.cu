@@ -224,7 +224,8 @@ __device__ __forceinline__ double face_momentum(const StepParams& p, const FaceK
     const double sq = sqrt(u0 * u0 + vt * vt);
     const double ram = friction(p, friction_coef(p, ib, ia), sq, hm);
     const double a = sw2d_half(dt2 * ram);
-    return ((1.00 - a) * q0 + (-along - across - g13)) / (1.00 + a);
+    /* the division on the integer pipes, correctly rounded (sw2d_div_rn) */
+    return sw2d_div_rn((1.00 - a) * q0 + (-along - across - g13), 1.00 + a);
 }
 
 __device__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* sm);
@@ -651,7 +652,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_update(StepParams p, in
                 if (r == 0) hm = shn[nr][nc];
                 else if (r == R) hm = shn[nr - 1][nc];
                 else hm = sw2d_half(shn[nr][nc] + shn[nr - 1][nc]);
-                p.uu1[i] = sw2d_ge_pos(hm, th) ? (sw2d_is0(F) ? F : F / hm) : 0.00; /* 0/hm is 0 of F's sign */
+                p.uu1[i] = sw2d_ge_pos(hm, th) ? (sw2d_is0(F) ? F : sw2d_div_rn(F, hm)) : 0.00; /* 0/hm is 0 of F's sign */
             }
             if (r < R) {
                 double F = fy[i];
@@ -661,7 +662,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_update(StepParams p, in
                 if (c == 0) hn = shn[nr][nc];
                 else if (c == C) hn = shn[nr][nc - 1];
                 else hn = sw2d_half(shn[nr][nc] + shn[nr][nc - 1]);
-                p.vv1[i] = sw2d_ge_pos(hn, th) ? (sw2d_is0(F) ? F : F / hn) : 0.0;
+                p.vv1[i] = sw2d_ge_pos(hn, th) ? (sw2d_is0(F) ? F : sw2d_div_rn(F, hn)) : 0.0;
             }
         }
     }
@@ -778,7 +779,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, i
         if (r == 0) hm = h[i];
         else if (r == p.R) hm = h[i - P];
         else hm = sw2d_half(h[i] + h[i - P]);
-        p.uu1[i] = sw2d_ge_pos(hm, th) ? (sw2d_is0(F) ? F : F / hm) : 0.00; /* 0/hm is 0 of F's sign */
+        p.uu1[i] = sw2d_ge_pos(hm, th) ? (sw2d_is0(F) ? F : sw2d_div_rn(F, hm)) : 0.00; /* 0/hm is 0 of F's sign */
     }
     if (r < p.R) {
         const double F = p.qy[0][i];
@@ -786,7 +787,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_facevel(StepParams p, i
         if (c == 0) hn = h[i];
         else if (c == p.C) hn = h[i - 1];
         else hn = sw2d_half(h[i] + h[i - 1]);
-        p.vv1[i] = sw2d_ge_pos(hn, th) ? (sw2d_is0(F) ? F : F / hn) : 0.0;
+        p.vv1[i] = sw2d_ge_pos(hn, th) ? (sw2d_is0(F) ? F : sw2d_div_rn(F, hn)) : 0.0;
     }
 }
 

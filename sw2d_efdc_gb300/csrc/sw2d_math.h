@@ -230,4 +230,80 @@ SW2D_HD double sw2d_rpow_manning(double x) {
     return sw2d_fma(w0, u, w0);
 }
 
+
+/* ------------------------------------------------------------------------
+ * a / b correctly rounded (round to nearest even) with integer and binary32
+ * operations only, for the GB300's FP64 pipe, which runs at 1/64 of the
+ * binary32 rate: a binary64 division there costs about as much as fifteen
+ * binary64 multiplies, while this schoolbook long division in base 2^22
+ * runs on the integer and binary32 pipes beside the step's other binary64
+ * work.  For a and b normal and a normal quotient (every other case returns
+ * the hardware a / b), with ma, mb the 53-bit significands scaled so that
+ * ma / mb is in [1, 2):
+ *   - quotient digits of 22, 22 and 10 bits, each estimated from the
+ *     leading 32 bits of the running remainder times a binary32 reciprocal
+ *     of mb (relative error ~2^-21, so the estimate is within a few units
+ *     of the digit), then made exact by the integer remainder
+ *     R' = R 2^k - d mb (computed modulo 2^64; the true value is below
+ *     4 mb < 2^56) and corrected by whole steps of mb until 0 <= R' < mb;
+ *   - the 55-bit quotient floor(ma 2^54 / mb) and the sticky bit R != 0
+ *     give the 53-bit significand rounded to nearest even.
+ * Being the correctly rounded quotient, the result is bit-identical to the
+ * IEEE division on any machine (the CPU tests compare it with the host's
+ * division over every class of operands). */
+SW2D_HD float sw2d_rcp_est(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / x;
+#endif
+}
+
+/* one base-2^k digit of R 2^k / mb: returns the digit, R becomes the new
+ * remainder; rfk = 2^(k-8) / (mb >> 29) estimated in binary32 */
+SW2D_HD uint32_t sw2d_div_digit(uint64_t* R, uint64_t mb, int k, float rfk) {
+    const uint64_t r = *R;
+    uint32_t d = (uint32_t)((float)(uint32_t)(r >> 21) * rfk); /* truncating conversion */
+    int64_t rn = (int64_t)((r << k) - (uint64_t)d * mb);        /* exact: |true value| < 2^56 */
+    while (rn < 0) {
+        d--;
+        rn += (int64_t)mb;
+    }
+    while (rn >= (int64_t)mb) {
+        d++;
+        rn -= (int64_t)mb;
+    }
+    *R = (uint64_t)rn;
+    return d;
+}
+
+SW2D_HD double sw2d_div_rn(double a, double b) {
+    const uint64_t ua = sw2d_f64_bits(a), ub = sw2d_f64_bits(b);
+    const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+    if (ea - 1u >= 0x7feu || eb - 1u >= 0x7feu) return a / b; /* zero, subnormal, inf, NaN */
+    const uint64_t M = (1ull << 52) - 1ull, H = 1ull << 52;
+    uint64_t ma = (ua & M) | H;
+    const uint64_t mb = (ub & M) | H;
+    int e = (int)ea - (int)eb + 1023;
+    if (ma < mb) {
+        ma <<= 1;
+        e -= 1;
+    }
+    if ((uint32_t)(e - 1) >= 0x7feu) return a / b; /* subnormal or overflowing quotient */
+    const float rf = sw2d_rcp_est((float)(uint32_t)(mb >> 29));
+    uint64_t R = ma - mb; /* the leading quotient bit is 1 */
+    const uint64_t d1 = sw2d_div_digit(&R, mb, 22, rf * 16384.0f);
+    const uint64_t d2 = sw2d_div_digit(&R, mb, 22, rf * 16384.0f);
+    const uint64_t d3 = sw2d_div_digit(&R, mb, 10, rf * 4.0f);
+    const uint64_t Q = H << 2 | d1 << 32 | d2 << 10 | d3; /* floor(ma 2^54 / mb), 55 bits */
+    uint64_t m = Q >> 2;
+    const uint64_t g = (Q >> 1) & 1ull, st = (Q & 1ull) | (R != 0 ? 1ull : 0ull);
+    m += g & (st | (m & 1ull));
+    /* the significand's leading bit carries into the exponent field; a
+     * significand rounded up to 2^53 carries once more */
+    return sw2d_f64_from_bits(((ua ^ ub) & (1ull << 63)) + ((uint64_t)(e - 1) << 52) + m);
+}
+
 #endif /* SW2D_MATH_H */

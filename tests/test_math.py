@@ -14,6 +14,7 @@ SRC = r"""
 #include "sw2d_math.h"
 void rpow(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_rpow_manning(x[i]); }
 void divc(const double* a, double d, double* y, long n) { double r = 1.0 / d; for (long i = 0; i < n; i++) y[i] = sw2d_div_const(a[i], d, r); }
+void divrn(const double* a, const double* b, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_div_rn(a[i], b[i]); }
 void lnf(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = (double)sw2d_ln_f32(x[i]); }
 void scal(const double* x, double* h, double* q, double* m0, long n) {
     for (long i = 0; i < n; i++) {
@@ -45,6 +46,7 @@ def mathlib(tmp_path_factory):
     L.rpow.argtypes = [dp, dp, ctypes.c_long]
     L.divc.argtypes = [dp, ctypes.c_double, dp, ctypes.c_long]
     L.lnf.argtypes = [dp, dp, ctypes.c_long]
+    L.divrn.argtypes = [dp, dp, dp, ctypes.c_long]
     L.scal.argtypes = [dp, dp, dp, dp, ctypes.c_long]
     L.cmps.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_int), ctypes.c_long]
     L.cmpp.argtypes = [dp, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.c_long]
@@ -178,3 +180,28 @@ def test_oracle_is_bit_identical_across_thread_counts():
             for k in ("h", "qx", "qy"):
                 assert np.array_equal(f[k], rs[0][2][k]), k
             assert led == rs[0][3]
+
+
+def test_integer_division_is_the_ieee_division(mathlib):
+    """sw2d_div_rn (long division on integer and binary32 operations) returns
+    the correctly rounded quotient, bit for bit the IEEE division, for
+    operands of every class (the special ones through the hardware
+    division), and for operands like the step's: a discharge over a face
+    depth or over 1 + a friction term."""
+    L, dp = mathlib
+    rng = np.random.default_rng(5)
+    n = 2_000_000
+    a = _all_classes(rng, n)
+    b = _all_classes(rng, n)
+    n = min(a.size, b.size)  # the class generator drops NaN patterns
+    a, b = np.ascontiguousarray(a[:n]), np.ascontiguousarray(b[:n])
+    k = n // 4
+    a[:k] = rng.standard_normal(k) * 10.0 ** rng.uniform(-8, 2, k)
+    b[:k] = 10.0 ** rng.uniform(-4, 1, k)
+    b[k:2 * k] = 1.0 + 10.0 ** rng.uniform(-12, 3, k)
+    y = np.empty(n)
+    L.divrn(a.ctypes.data_as(dp), b.ctypes.data_as(dp), y.ctypes.data_as(dp), n)
+    with np.errstate(all="ignore"):
+        ref = a / b
+    same = (y.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(y) & np.isnan(ref))
+    assert same.all(), (a[~same][:3], b[~same][:3], y[~same][:3], ref[~same][:3])
