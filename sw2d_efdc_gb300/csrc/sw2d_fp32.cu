@@ -64,6 +64,7 @@ struct SmemM {
     int srow[T32_MAXSRC], scol[T32_MAXSRC];
     float sq1[T32_MAXSRC], sq2[T32_MAXSRC];
     unsigned q;                 /* queue ticket of the item in hand (~0u: leave) */
+    unsigned qn;                /* the ticket drawn ahead for the next item */
     int last;                   /* this CTA finished its scenario's iteration */
     ClsStage cls[NS];
     RwStage rw[NS];
@@ -785,16 +786,18 @@ __device__ void prepare_slot32(const Scn32& P, volatile Clock32* clk, double t, 
     if (!active) clk->done = 1;
 }
 
-/* One scenario's end of iteration, run by one warp: fixed-order sum of its
- * work items' partials (read past L1: other CTAs wrote them during this
- * launch), ledger, clock, outlet record and the next slot. */
-__device__ __noinline__ void finalize_scn(const Scn32& P, const Part32* __restrict__ part) {
-    const int lane = threadIdx.x & 31;
+/* One scenario's end of iteration, run by the whole CTA: fixed-order sum of
+ * its work items' partials (each thread a fixed stride of them, then the
+ * warps and the CTA in a fixed order; read past L1: other CTAs wrote them
+ * during this launch), then, by thread 0, the ledger, clock, outlet record
+ * and the next slot. */
+__device__ __noinline__ void finalize_scn(const Scn32& P, const Part32* __restrict__ part, double (*red)[4],
+                                          float (*redf)[2]) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     volatile Clock32* clk = P.clk;
-    if (!clk->slot.active) return;
     double clamp = 0, qout = 0, rain = 0, evc = 0;
     float sx = 0.f, sy = 0.f;
-    for (int k = lane; k < P.nwork; k += 32) {
+    for (int k = tid; k < P.nwork; k += NT) {
         const Part32* q = part + P.first_work + k;
         clamp += __ldcg(&q->clamp);
         qout += __ldcg(&q->qout);
@@ -812,7 +815,24 @@ __device__ __noinline__ void finalize_scn(const Scn32& P, const Part32* __restri
         sx = fmaxf(sx, __shfl_down_sync(0xffffffffu, sx, o));
         sy = fmaxf(sy, __shfl_down_sync(0xffffffffu, sy, o));
     }
-    if (lane != 0) return;
+    if (lane == 0) {
+        red[warp][0] = clamp;
+        red[warp][1] = qout;
+        red[warp][2] = rain;
+        red[warp][3] = evc;
+        redf[warp][0] = sx;
+        redf[warp][1] = sy;
+    }
+    __syncthreads();
+    if (tid != 0 || !clk->slot.active) return;
+    for (int k = 1; k < NW; k++) {
+        clamp += red[k][0];
+        qout += red[k][1];
+        rain += red[k][2];
+        evc += red[k][3];
+        sx = fmaxf(sx, redf[k][0]);
+        sy = fmaxf(sy, redf[k][1]);
+    }
     const float rr2 = clk->slot.rr2, ev2 = clk->slot.ev2;
     const int cur = clk->slot.cur;
     const double dt2 = clk->dt2;
@@ -855,15 +875,17 @@ __device__ __forceinline__ void st_release_gpu(int* p, int v) {
     asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-/* The queue side of the persistent loop, run by thread 0: the next ticket
- * and the bounded wait for its scenario's previous iteration.  Returns the
- * ticket, or ~0u when the CTA is to leave (the queue is empty, or a wait
- * ran out: then the scenario's timeout bit and the abort flag are set). */
-__device__ __noinline__ unsigned fetch_ticket(const Scn32* __restrict__ scns, const int4* __restrict__ work, int nwork,
-                                              int niter, Ctl32* ctl) {
+/* The queue side of the persistent loop, run by thread 0: the bounded wait
+ * of ticket q (drawn ahead, while the CTA worked on its previous item) for
+ * its scenario's previous iteration.  Returns the ticket, or ~0u when the
+ * CTA is to leave (the queue is empty, or a wait ran out: then the
+ * scenario's timeout bit and the abort flag are set).  A waiting ticket only
+ * ever waits for smaller tickets, so holding one ticket ahead cannot close a
+ * cycle of waits. */
+__device__ __noinline__ unsigned wait_ticket(unsigned q, const Scn32* __restrict__ scns,
+                                             const int4* __restrict__ work, int nwork, int niter, Ctl32* ctl) {
     const int* done = reinterpret_cast<const int*>(ctl + 1);
     volatile unsigned* abort_flag = &ctl->abort;
-    const unsigned q = atomicAdd(&ctl->next, 1u);
     if (q >= (unsigned)nwork * (unsigned)niter || *abort_flag) return ~0u;
     const int it = (int)(q / (unsigned)nwork);
     const int sc = work[q % (unsigned)nwork].x;
@@ -875,7 +897,7 @@ __device__ __noinline__ unsigned fetch_ticket(const Scn32* __restrict__ scns, co
             *abort_flag = 1u;
             return ~0u;
         }
-        __nanosleep(100);
+        __nanosleep(64);
     }
     return q;
 }
@@ -922,8 +944,9 @@ __global__ void __launch_bounds__(NT, 4) k32_persist(const Scn32* __restrict__ s
     }
     __syncthreads();
     unsigned gb = 0; /* staged blocks used so far by this CTA */
+    if (threadIdx.x == 0) S.qn = atomicAdd(&ctl->next, 1u);
     for (;;) {
-        if (threadIdx.x == 0) S.q = fetch_ticket(scns, work, nwork, niter, ctl);
+        if (threadIdx.x == 0) S.q = wait_ticket(S.qn, scns, work, nwork, niter, ctl);
         __syncthreads();
         /* read through a shuffle from lane 0: the compiler then knows the
          * ticket, the item and the scenario's fields are uniform across the
@@ -931,6 +954,7 @@ __global__ void __launch_bounds__(NT, 4) k32_persist(const Scn32* __restrict__ s
          * thread to the marching windows */
         const unsigned q = __shfl_sync(0xffffffffu, S.q, 0);
         if (q == ~0u) break;
+        if (threadIdx.x == 0) S.qn = atomicAdd(&ctl->next, 1u); /* the next ticket, drawn while this item runs */
         const int4 w = work[q % (unsigned)nwork];
         /* the previous iteration's state was written by other CTAs with
          * generic stores; this item reads it with TMA (the async proxy) */
@@ -941,9 +965,9 @@ __global__ void __launch_bounds__(NT, 4) k32_persist(const Scn32* __restrict__ s
         }
         if (threadIdx.x == 0) S.last = count_item(scns, nscn, w.x, ctl);
         __syncthreads();
-        if (__shfl_sync(0xffffffffu, S.last, 0) && threadIdx.x < 32) {
+        if (__shfl_sync(0xffffffffu, S.last, 0)) {
             __threadfence();
-            finalize_scn(scns[w.x], part);
+            finalize_scn(scns[w.x], part, S.red, S.redf);
             if (threadIdx.x == 0) release_scenario(nscn, w.x, (int)(q / (unsigned)nwork) + 1, ctl);
         }
         __syncthreads();
