@@ -339,11 +339,10 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
     }
     /* datums of the bands the staged rows span, for the strips west, own
      * and east (0 outside the raster) */
-    const int b0 = max(Ls, 0) / M_DR;
-    const int nband = min(re + 2, R - 1) / M_DR - b0 + 1;
-    if (tid < 3 * nband) {
+    if (tid < 3 * M_MAXBANDS) {
+        const int b0 = max(Ls, 0) / M_DR;
         const int j = tid / 3, cr = tid - 3 * j, nx = strip + cr - 1;
-        S.dband[j][cr] = (nx >= 0 && nx < P.tiles_x) ? P.datum[(b0 + j) * P.tiles_x + nx] : 0.f;
+        S.dband[j][cr] = (nx >= 0 && nx < P.tiles_x && b0 + j < P.bands) ? P.datum[(b0 + j) * P.tiles_x + nx] : 0.f;
     }
     __syncthreads();
     constexpr bool has_cls = CLS, has_rw = RW;
@@ -408,6 +407,10 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
         ACT[k] = ACTL[k] = DRY[k] = 0;
     }
     float2 Zp = f2(0.f); /* bed offsets of the row above */
+    /* datum band of the row in hand, counted from the band of the first staged
+     * row; it grows by one at each band edge (rows past the last band are
+     * the halo, whose bed is NaN whatever its datum) */
+    int bj = 0;
     float clamp = 0.f, qout = 0.f, rainacc = 0.f, evc = 0.f;
     float sxm = 0.f, sym = 0.f;
     const int nls = SRC ? S.nls : 0;
@@ -482,9 +485,9 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
             /* bed steps of the x face north of row L and the y faces west of
              * its cells, plus the datum step where the face crosses a datum
              * tile's edge (a band edge above row L, a strip edge west) */
-            const int bj = min(max(L, 0) / M_DR - b0, nband - 1);
             float2 dzx = sub2(z0, Zp);
-            if ((L & (M_DR - 1)) == 0 && L > 0 && L < R) {
+            if ((L & (M_DR - 1)) == 0 && L > 0) { /* a band edge above row L */
+                bj++;
                 const float c = S.dband[bj][creg] - S.dband[bj - 1][creg];
                 dzx = add2(dzx, f2(c));
             }

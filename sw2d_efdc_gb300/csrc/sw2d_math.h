@@ -11,7 +11,8 @@
  *     ram = gg*rn*rn*sqx / pow(hm, 1.3333330)        (SW2D-EFDC.cu:193-195, :310-312)
  * On GB300 the FP64 pipe is ~1/64 of the FP32 rate, so the library pow
  * (an extended-precision log/exp) dominates the FP64 step.  sw2d_rpow_manning()
- * returns hm^-1.333333 to a few ulp from a short published construction:
+ * returns hm^-1.333333 to a few ulp from a short published construction,
+ * evaluated in pairs of binary32 numbers (only two binary64 additions):
  *   - x^(-1/3) by Newton's iteration for f(r) = x r^3 - 1 in binary32, seeded
  *     by the exponent-scaling bit trick (Blinn, "Floating-point tricks",
  *     IEEE CG&A 1997);
@@ -211,14 +212,15 @@ SW2D_HD float sw2d_ln_f32(double x) {
     return sw2d_fmaf(kf, 0.693145751953125f, sw2d_fmaf(kf, 1.428606820309417e-06f, lnm));
 }
 
-/* hm^(-1.3333330), the reciprocal of the reference's pow(hm, 1.3333330).
+/* hm^(-1.3333330), the reciprocal of the reference's pow(hm, 1.3333330),
+ * binary64 throughout: the form used outside the range of
+ * sw2d_rpow_manning below.
  * With r0 the binary32 seed (exact in binary64, so r0^2 is exact) and
  * e = 1 - x r0^3, x^(-4/3) = r0^4 (1 - e)^(-4/3) = r0^4 (1 + 4e/3 + 14e^2/9 + O(e^3));
  * the residual exponent contributes x^(-d) = (1 + t + t^2/2), t = -d ln x,
  * |t| < 4e-6, with ln x from sw2d_ln_f32 (its 6e-7 error moves t by 2e-13);
- * both corrections are folded into one fma.  Relative error < 3e-13; only
- * fifteen operations run on the binary64 pipe. */
-SW2D_HD double sw2d_rpow_manning(double x) {
+ * both corrections are folded into one fma.  Relative error < 3e-13. */
+SW2D_HD double sw2d_rpow_manning_f64(double x) {
     double r0 = (double)sw2d_rcbrt_seed((float)x);
     double r2 = r0 * r0;
     double w0 = r2 * r2;
@@ -230,6 +232,48 @@ SW2D_HD double sw2d_rpow_manning(double x) {
     return sw2d_fma(w0, u, w0);
 }
 
+/* hm^(-1.3333330) with the same construction carried in pairs of binary32
+ * numbers (a value and its rounding error, Dekker's products by fma and
+ * Knuth's TwoSum), so that only the last two additions run on the binary64
+ * pipe (GB300: 1/64 of the binary32 rate):
+ *   x = xh + xl split by integer operations (xh its leading 24 significand
+ *   bits, exact in binary32);
+ *   r0^2 = r2h + r2l and r0^4 exact or to 2^-48 relative by fma products;
+ *   e = 1 - x r0^3 in one binary32 (|e| ~ 2^-21, absolute error ~2^-46);
+ *   t = c ln x as a pair, c = 1.3333330 - 4/3 split into two binary32;
+ *   u = (1 + 4e/3 + 14e^2/9)(1 + t + t^2/2) - 1 as the pair (s, ul);
+ *   result w0 (1 + u) assembled in binary64 from three binary32 terms.
+ * Relative error < 3e-13 of pow (the CPU test bounds it on 1e-4 <= x <=
+ * 1e3); outside 2^-60 <= x < 2^61 the binary64 form above is used.  Only
+ * IEEE binary32 +, -, *, fma, integer operations and exact conversions
+ * appear, so host and device agree bit for bit. */
+SW2D_HD double sw2d_rpow_manning(double x) {
+    const uint64_t b = sw2d_f64_bits(x);
+    const int ex = (int)((b >> 52) & 0x7ff);
+    if (ex < 1023 - 60 || ex > 1023 + 60) return sw2d_rpow_manning_f64(x);
+    const float xh = sw2d_f32_from_bits((uint32_t)((ex - 896) << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
+    const float xl = (float)(uint32_t)(b & 0x1fffffffu) * sw2d_f32_from_bits((uint32_t)(ex - 1075 + 127) << 23);
+    const float r0 = sw2d_rcbrt_seed(xh);
+    const float r2h = r0 * r0, r2l = sw2d_fmaf(r0, r0, -r2h);
+    const float r3h = r2h * r0, r3l = sw2d_fmaf(r2h, r0, -r3h) + r2l * r0;
+    const float P = xh * r3h;
+    const float Pe = sw2d_fmaf(xh, r3h, -P);
+    const float e = (1.0f - P) - (Pe + (xh * r3l + xl * r3h)); /* 1 - P is exact: P is within 2^-21 of 1 */
+    const float a4 = e * sw2d_fmaf(e, 1.5555556f, 1.3333334f);
+    const float ln = sw2d_ln_f32(x);
+    const float th = 3.3333333249174757e-07f * ln;
+    const float tl = sw2d_fmaf(3.3333333249174757e-07f, ln, -th) + 7.40148665436918e-16f * ln;
+    const float fl = tl + 0.5f * th * th;
+    const float s = th + a4; /* TwoSum(th, a4) */
+    const float bb = s - th;
+    const float ul = ((th - (s - bb)) + (a4 - bb)) + fl + a4 * th;
+    const float w0h = r2h * r2h;
+    const float w0l = sw2d_fmaf(r2h, r2h, -w0h) + 2.0f * r2h * r2l;
+    const float ph = w0h * s;
+    const float pl = sw2d_fmaf(w0h, s, -ph);
+    const float rest = pl + w0l + w0h * ul + w0l * s;
+    return (double)w0h + ((double)ph + (double)rest);
+}
 
 /* ------------------------------------------------------------------------
  * a / b correctly rounded (round to nearest even) with integer and binary32
