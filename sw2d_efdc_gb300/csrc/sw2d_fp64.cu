@@ -200,14 +200,14 @@ __device__ __forceinline__ FaceK classify(bool act, double ha, double hb, const 
 /* discharge of a non-momentum face */
 __device__ __forceinline__ double face_special(const FaceK& f, double th, double gg) {
     switch (f.kind) {
-    case 2: return f.wa ? 0.5440 * f.ha * sqrt(gg * f.ha) : 0.0;
-    case 3: return f.wb ? -0.544 * f.hb * sqrt(gg * f.hb) : 0.0;
+    case 2: return f.wa ? 0.5440 * f.ha * sw2d_sqrt_rn(gg * f.ha) : 0.0;
+    case 3: return f.wb ? -0.544 * f.hb * sw2d_sqrt_rn(gg * f.hb) : 0.0;
     case 4:
         if (sw2d_gt0(f.hb) || sw2d_gt0(f.ha)) {
             const double hhan = (f.hb - th) - (f.ha - th);
             const double sgnm = copysign(1.0, hhan);
             const double hh3 = fmax(f.hhb, f.hha) - fmax(f.zb, f.za);
-            return -sgnm * 0.350 * hh3 * sqrt(2.00 * gg * hh3);
+            return -sgnm * 0.350 * hh3 * sw2d_sqrt_rn(2.00 * gg * hh3);
         }
         return 0.0;
     default: return 0.0;
@@ -221,7 +221,7 @@ __device__ __forceinline__ double face_momentum(const StepParams& p, const FaceK
                                                 double dt2, double dt2n, size_t ia, size_t ib) {
     const double gg = p.g;
     const double g13 = gg * hm * dt2n * (f.hhb - f.ha - f.za);
-    const double sq = sqrt(u0 * u0 + vt * vt);
+    const double sq = sw2d_sqrt_rn(u0 * u0 + vt * vt); /* on the integer pipes, correctly rounded */
     const double ram = friction(p, friction_coef(p, ib, ia), sq, hm);
     const double a = sw2d_half(dt2 * ram);
     /* the division on the integer pipes, correctly rounded (sw2d_div_rn) */
@@ -235,7 +235,7 @@ __device__ float block_max_f32_all(float v, float* sm);
  * sqrt(g * mean depth)) / spacing for faces between two active cells whose
  * mean depth is >= th (the oracle's cfl_speed, same operations). */
 __device__ __forceinline__ double face_speed(double vel, double hm, double g, double rd) {
-    return (fabs(vel) + sqrt(g * hm)) * rd;
+    return (fabs(vel) + sw2d_sqrt_rn(g * hm)) * rd;
 }
 
 /* exact block maximum of face speeds: binary32 estimate for every face,
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, i
                 double F;
                 if (edgeS) { /* south edge: free overfall when open */
                     const double hw = h[i - P];
-                    F = ((p.flags[i - P] & SW2D_F_ACTIVE) && sw2d_gt_pos(hw, th)) ? 0.5440 * hw * sqrt(gg * hw)
+                    F = ((p.flags[i - P] & SW2D_F_ACTIVE) && sw2d_gt_pos(hw, th)) ? 0.5440 * hw * sw2d_sqrt_rn(gg * hw)
                                                                                      : 0.0;
                 } else if (fx.kind == 1) {
                     const double u11 = dt2dx * (sea[ty + 1][tx] - sea[ty][tx]);

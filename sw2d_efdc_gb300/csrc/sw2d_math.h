@@ -350,4 +350,85 @@ SW2D_HD double sw2d_div_rn(double a, double b) {
     return sw2d_f64_from_bits(((ua ^ ub) & (1ull << 63)) + ((uint64_t)(e - 1) << 52) + m);
 }
 
+/* ------------------------------------------------------------------------
+ * sqrt(x) correctly rounded with integer and binary32 operations only (the
+ * companion of sw2d_div_rn), for x positive and normal (every other x
+ * returns the hardware sqrt).  With x = m 2^E, E even, m in [2^52, 2^54):
+ *   - an estimate S0 of S = floor(sqrt(m 2^56)) (55 bits) from sqrt(f),
+ *     f = m / 2^52, in a pair of binary32 numbers: a binary32 square root
+ *     and one Newton correction (error ~2^-46, S0 within a few hundred units);
+ *   - one correction by the exact 128-bit remainder N - S0^2 over 2 S0
+ *     (binary32 estimate, S1 within a couple of units), then whole steps on
+ *     the exact 64-bit remainder until 0 <= N - S^2 <= 2 S;
+ *   - S and the sticky bit N - S^2 != 0 give the 53-bit significand rounded
+ *     to nearest even (a square root is never exactly halfway).
+ * Bit-identical to the IEEE square root (the CPU tests compare it with the
+ * host's sqrt). */
+SW2D_HD uint64_t sw2d_umulhi(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+SW2D_HD float sw2d_sqrt_est(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return sqrtf(x);
+#endif
+}
+
+SW2D_HD double sw2d_sqrt_rn(double x) {
+    const uint64_t ux = sw2d_f64_bits(x);
+    const uint32_t ex = (uint32_t)(ux >> 52);
+    if (ex - 1u >= 0x7feu) return sqrt(x); /* negative, zero, subnormal, inf, NaN */
+    const uint64_t H = 1ull << 52;
+    uint64_t m = (ux & (H - 1ull)) | H;
+    int E = (int)ex - 1075; /* x = m 2^E */
+    if (E & 1) {
+        m <<= 1;
+        E -= 1;
+    }
+    /* f = m / 2^52 in [1, 4) as fh + fl: fh its leading 24 bits (exact) */
+    const int big = (int)(m >> 53); /* f >= 2 */
+    const uint64_t mt = m >> (29 + big), ml = m & ((1ull << (29 + big)) - 1ull);
+    const float fh = sw2d_f32_from_bits(((uint32_t)(127 + big) << 23) | ((uint32_t)mt & 0x7fffffu));
+    const float fl = (float)(uint32_t)ml * sw2d_f32_from_bits((uint32_t)(127 - 52) << 23);
+    const float sh = sw2d_sqrt_est(fh);
+    const float d = sw2d_fmaf(-sh, sh, fh) + fl;      /* f - sh^2 */
+    const float corr = d * (0.5f * sw2d_rcp_est(sh)); /* Newton: sqrt(f) ~ sh + d / (2 sh) */
+    /* S0 = (sh + corr) 2^54: sh has 24 significant bits, so sh 2^54 is an integer */
+    const uint32_t sb = sw2d_f32_bits(sh);
+    const int se = (int)(sb >> 23) - 127; /* sh in [1, 2): se = 0 (or 1 when sh rounds to 2) */
+    const uint64_t s_int = ((uint64_t)((sb & 0x7fffffu) | 0x800000u)) << (31 + se);
+    uint64_t S = s_int + (uint64_t)(int64_t)(corr * 18014398509481984.0f); /* corr 2^54 */
+    /* exact remainder N - S^2 in 128 bits, N = m 2^56 */
+    const uint64_t nh = m >> 8, nl = m << 56;
+    const uint64_t sl = S * S, sh2 = sw2d_umulhi(S, S);
+    const uint64_t rl = nl - sl;
+    const uint64_t rh = nh - sh2 - (nl < sl ? 1ull : 0ull);
+    /* r / 2^8 fits in a signed 64-bit number (|r| < 2^70) */
+    const int64_t r8 = (int64_t)((rh << 56) | (rl >> 8));
+    const float dl = (float)r8 * 256.0f * (0.5f * sw2d_rcp_est((float)S));
+    S += (uint64_t)(int64_t)dl;
+    int64_t r = (int64_t)((m << 56) - S * S); /* exact: |N - S^2| < 2^60 now */
+    while (r < 0) {
+        S--;
+        r += (int64_t)(2 * S + 1);
+    }
+    while (r > (int64_t)(2 * S)) {
+        r -= (int64_t)(2 * S + 1);
+        S++;
+    }
+    uint64_t q = S >> 2;
+    const uint64_t g = (S >> 1) & 1ull, st = (S & 1ull) | (r != 0 ? 1ull : 0ull);
+    q += g & (st | (q & 1ull));
+    const int eb = (E + 52) / 2 + 1023;
+    return sw2d_f64_from_bits(((uint64_t)(eb - 1) << 52) + q);
+}
+
 #endif /* SW2D_MATH_H */

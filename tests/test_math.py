@@ -14,6 +14,7 @@ SRC = r"""
 #include "sw2d_math.h"
 void rpow(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_rpow_manning(x[i]); }
 void divc(const double* a, double d, double* y, long n) { double r = 1.0 / d; for (long i = 0; i < n; i++) y[i] = sw2d_div_const(a[i], d, r); }
+void sqrtrn(const double* a, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_sqrt_rn(a[i]); }
 void divrn(const double* a, const double* b, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_div_rn(a[i], b[i]); }
 void lnf(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = (double)sw2d_ln_f32(x[i]); }
 void scal(const double* x, double* h, double* q, double* m0, long n) {
@@ -47,6 +48,7 @@ def mathlib(tmp_path_factory):
     L.divc.argtypes = [dp, ctypes.c_double, dp, ctypes.c_long]
     L.lnf.argtypes = [dp, dp, ctypes.c_long]
     L.divrn.argtypes = [dp, dp, dp, ctypes.c_long]
+    L.sqrtrn.argtypes = [dp, dp, ctypes.c_long]
     L.scal.argtypes = [dp, dp, dp, dp, ctypes.c_long]
     L.cmps.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_int), ctypes.c_long]
     L.cmpp.argtypes = [dp, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.c_long]
@@ -205,3 +207,24 @@ def test_integer_division_is_the_ieee_division(mathlib):
         ref = a / b
     same = (y.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(y) & np.isnan(ref))
     assert same.all(), (a[~same][:3], b[~same][:3], y[~same][:3], ref[~same][:3])
+
+
+def test_integer_square_root_is_the_ieee_square_root(mathlib):
+    """sw2d_sqrt_rn (integer and binary32 operations) returns the correctly
+    rounded square root, bit for bit the IEEE one, for every class of
+    operand, for squares of integers and their neighbours, and for operands
+    like the step's (u^2 + v^2 of face velocities, g h)."""
+    L, dp = mathlib
+    rng = np.random.default_rng(6)
+    a = _all_classes(rng, 2_000_000)
+    k = a.size // 4
+    a[:k] = np.abs(rng.standard_normal(k)) * 10.0 ** rng.uniform(-20, 3, k)
+    sq = np.arange(1, k + 1, dtype=np.float64) ** 2
+    a[k:2 * k] = (sq.view(np.uint64) + rng.integers(-2, 3, k).astype(np.uint64)).view(np.float64)
+    a = np.ascontiguousarray(a)
+    y = np.empty_like(a)
+    L.sqrtrn(a.ctypes.data_as(dp), y.ctypes.data_as(dp), a.size)
+    with np.errstate(all="ignore"):
+        ref = np.sqrt(a)
+    same = (y.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(y) & np.isnan(ref))
+    assert same.all(), (a[~same][:3], y[~same][:3], ref[~same][:3])
