@@ -1,5 +1,5 @@
-/* FP32 precision form of the SW2D step on sm_103a: one row-marching kernel
- * per iteration.
+/* FP32 precision form of the SW2D step on sm_103a: one persistent,
+ * row-marching kernel per chunk of iterations.
  *
  * A work item is a 224-column strip x `seg` rows of one scenario, taken by a
  * CTA of four warps.  Thread 0 streams the strip's rows (232 columns with a
@@ -18,9 +18,11 @@
  *            written back with its north and west faces.
  * There is no index arithmetic per cell and no barrier per row; halo rows
  * and columns are recomputed instead of exchanged, so an iteration reads
- * every field once from HBM and writes it once.  A second, tiny kernel
- * reduces each scenario's work-item partials in a fixed order and prepares
- * the scenario's next iteration (CFL length, rain).
+ * every field once from HBM and writes it once.  CTAs take work items of
+ * every scenario and iteration of the chunk from a device queue; the CTA
+ * that finishes a scenario's last item of an iteration reduces its partials
+ * in a fixed order, prepares the scenario's next iteration (CFL length,
+ * rain) and releases it to the items waiting on it (k32_persist).
  *
  * Arithmetic is binary32 except the clock, the ledger and the CFL length
  * (binary64).  Gravity uses (h_e - h_w) + (z_e - z_w) with bed offsets from

@@ -250,7 +250,7 @@ __device__ __forceinline__ unsigned long long block_face_speed_max(bool ok, doub
     return block_max_u64(bits, smu);
 }
 
-__global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 4) k64_flux(StepParams p, int cur) {
+__global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 3) k64_flux(StepParams p, int cur) {
     __shared__ float smf[SW2D_BX * SW2D_BY / 32];
     __shared__ unsigned long long smu[SW2D_BX * SW2D_BY / 32];
     /* momentum faces of the block, then the edges of the block's cells and of
