@@ -417,16 +417,24 @@ def fp32_only_cells(res, tol=PREC_TOL_M, base="fp64", fp32="fp32"):
         for j in pert:
             if j != k:
                 rest |= over[j]
+        own_k, f32_k = over[k] & ~rest, over[fp32] & ~rest
         out["perturbations"][k] = {
             "cells_over_tol": int(over[k].sum()), "fp32_cells_also_here": int((over[fp32] & over[k]).sum()),
-            "own_cells_unexplained_by_the_others": int((over[k] & ~rest).sum()),
-            "fp32_cells_unexplained_by_the_others": int((over[fp32] & ~rest).sum())}
+            "own_cells_unexplained_by_the_others": int(own_k.sum()),
+            "fp32_cells_unexplained_by_the_others": int(f32_k.sum()),
+            # the largest peak-depth error among those cells, the run's own / the FP32 form's
+            "own_worst_unexplained_m": float(err[k][own_k].max()) if own_k.any() else 0.0,
+            "fp32_worst_unexplained_m": float(err[fp32][f32_k].max()) if f32_k.any() else 0.0}
     own = [v["own_cells_unexplained_by_the_others"] for v in out["perturbations"].values()]
     f32 = [v["fp32_cells_unexplained_by_the_others"] for v in out["perturbations"].values()]
     if own:
+        ow = [v["own_worst_unexplained_m"] for v in out["perturbations"].values()]
+        fw = [v["fp32_worst_unexplained_m"] for v in out["perturbations"].values()]
         out["leave_one_out"] = {"perturbed_runs_min": min(own), "perturbed_runs_max": max(own),
                                 "perturbed_runs_mean": float(np.mean(own)), "fp32_mean": float(np.mean(f32)),
-                                "fp32_within_perturbed_range": bool(min(own) <= np.mean(f32) <= max(own))}
+                                "fp32_within_perturbed_range": bool(min(own) <= np.mean(f32) <= max(own)),
+                                "perturbed_worst_m_min": min(ow), "perturbed_worst_m_max": max(ow),
+                                "fp32_worst_m_mean": float(np.mean(fw))}
     d = err[fp32]
     spread = np.zeros_like(d)
     for k in pert:
@@ -519,13 +527,14 @@ def run_batched_leg(args, peak, fp64_value):
     achieved = value * (BYTES_PER_CELL_FP32_CFG3 + 1)  # + the class byte
     return {"value": round(value, 4), "unit": UNIT, "scenarios": len(specs), "cells": int(cells),
             "steps": args.steps, "ms_per_step": round(ms / args.steps, 4),
-            "rows_per_item": st1["rows_per_item"], "tuning_ms": round(st1["tuning_ms"], 1),
+            "rows_per_item": st1["rows_per_item"], "ctas_per_sm": st1["ctas_per_sm"] or "all",
+            "tuning_ms": round(st1["tuning_ms"], 1),
             "launches": int(st1["launches"] - st0["launches"]),
             "workload": "batched FP32: %d scenarios, side log-uniform 128-2048, fractal DEM, 3-class Voronoi n, "
                         "gamma hyetographs, per-scenario CFL length; one persistent cooperative launch per chunk "
                         "of up to 32 iterations (every scenario has a class raster: one feature class), each "
-                        "scenario's iterations chained on the device; rows per work item chosen by the "
-                        "autotuner (%d)" % (len(specs), st1["rows_per_item"]),
+                        "scenario's iterations chained on the device; rows per work item and CTAs per SM chosen "
+                        "by the autotuner (%d, %s)" % (len(specs), st1["rows_per_item"], st1["ctas_per_sm"] or "all"),
             "roofline": {"bound": "hbm", "kernel": "k32_persist", "achieved": round(achieved, 2),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3 + 1},
@@ -584,7 +593,8 @@ def run_served_leg(args, fp64_value):
             "value": round(stats["cell_updates"] / (stats["device_ms"] * 1e-3) / 1e9, 4), "unit": UNIT,
             "vs_fp64_plain": round(stats["cell_updates"] / (stats["device_ms"] * 1e-3) / 1e9 / fp64_value, 3)
             if fp64_value else None,
-            "tuning_s": round(stats["tuning_ms"] / 1e3, 3), "rows_per_item": stats["rows_per_item"],
+            "tuning_s": round(stats["tuning_ms"] / 1e3, 3), "size_buckets_tuned": stats["tunings"],
+            "rows_per_item": stats["rows_per_item"], "ctas_per_sm": stats["ctas_per_sm"] or "all",
             "workload": "served FP32: Poisson arrivals 20/s, side log-uniform 256-4096, durations U(1,6) h x %g, "
                         "HBM budget 150 GB, continuous admission" % args.serve_time_scale,
             "input_generation_s": round(gen_s, 1)}

@@ -60,6 +60,9 @@ typedef struct sw2d_batch_stats {
     double launches;          /* kernel launches issued (one persistent launch per feature class and chunk) */
     double tuning_ms;         /* host time the autotuner spent timing candidate work items (its timed
                                  iterations advanced the scenarios like any other) */
+    int ctas_per_sm;          /* CTAs per SM of the persistent launches (the autotuner's choice; 0 = all
+                                 that fit) */
+    int tunings;              /* size buckets the autotuner has timed (each is cached) */
 } sw2d_batch_stats;
 
 typedef struct sw2d_batch sw2d_batch;

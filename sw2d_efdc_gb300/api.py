@@ -73,7 +73,8 @@ class Scenario(C.Structure):
 class BatchStats(C.Structure):
     _fields_ = [("running", C.c_int), ("queued", C.c_int), ("work_items", C.c_int), ("rows_per_item", C.c_int),
                 ("bytes_in_use", C.c_double), ("device_ms", C.c_double), ("cell_updates", C.c_double),
-                ("launches", C.c_double), ("tuning_ms", C.c_double)]
+                ("launches", C.c_double), ("tuning_ms", C.c_double),
+                ("ctas_per_sm", C.c_int), ("tunings", C.c_int)]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3

@@ -372,6 +372,8 @@ int sw2d_batch_get_stats(sw2d_batch* b, sw2d_batch_stats* out) {
     out->work_items = b->eng->nwork();
     out->rows_per_item = b->eng->segment_rows();
     out->tuning_ms = b->eng->tuning_ms();
+    out->ctas_per_sm = b->eng->ctas_per_sm();
+    out->tunings = b->eng->tunings();
     return SW2D_OK;
 }
 

@@ -468,12 +468,18 @@ int Engine32::rebuild(std::string* err) {
     return SW2D_OK;
 }
 
-/* niter iterations: one persistent launch per feature class present, each
- * with as many CTAs as its SMs hold (at most one per queue ticket) */
+/* CTAs of class k's persistent launch over niter iterations: the CTAs per
+ * SM in use (at most what the SM holds) on every SM, at most one per queue
+ * ticket */
+int Engine32::grid_of(int k, int niter) const {
+    const int per_sm = cps_ > 0 ? std::min(cps_, bps_[k]) : bps_[k];
+    return (int)std::max<long long>(1, std::min<long long>((long long)per_sm * nsm_, (long long)class_n_[k] * niter));
+}
+
+/* niter iterations: one persistent launch per feature class present */
 int Engine32::launch(int niter, std::string* err) {
     int grid[T32_NCLASS];
-    for (int k = 0; k < T32_NCLASS; k++)
-        grid[k] = (int)std::max<long long>(1, std::min<long long>((long long)bps_[k] * nsm_, (long long)class_n_[k] * niter));
+    for (int k = 0; k < T32_NCLASS; k++) grid[k] = grid_of(k, niter);
     ECK(fp32_launch_chunk(d_scn_, (int)scn_.size(), d_work_, class_first_, class_n_, d_part_, d_ctl_, niter, grid,
                           stream_));
     return SW2D_OK;
@@ -484,8 +490,7 @@ int Engine32::build_graph(std::string* err) {
     cudaGraph_t g = nullptr;
     ECK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     int grid[T32_NCLASS];
-    for (int k = 0; k < T32_NCLASS; k++)
-        grid[k] = (int)std::max<long long>(1, std::min<long long>((long long)bps_[k] * nsm_, (long long)class_n_[k] * kChunk));
+    for (int k = 0; k < T32_NCLASS; k++) grid[k] = grid_of(k, kChunk);
     cudaError_t el = fp32_launch_chunk(d_scn_, (int)scn_.size(), d_work_, class_first_, class_n_, d_part_, d_ctl_, kChunk,
                                        grid, stream_);
     cudaError_t ec = cudaStreamEndCapture(stream_, &g);
@@ -507,36 +512,51 @@ int Engine32::tune(std::string* err, long long* advanced) {
     double cells = 0;
     for (auto& sp : scn_) cells += (double)sp->R * sp->C;
     if (seg_fixed_ > 0 || cells < (1 << 20)) return SW2D_OK;
-    if (tuned_cells_ > 0 && cells <= 2.0 * tuned_cells_ && cells >= 0.5 * tuned_cells_) return SW2D_OK;
-    const auto t0 = std::chrono::steady_clock::now();
-    int best = seg_;
-    float best_ms = 3.4e38f;
+    const int bucket = (int)std::floor(std::log2(cells));
+    if (bucket == bucket_) return SW2D_OK;
     int rc;
-    for (int cand : {64, 128, 256, 512}) {
-        if (cand != seg_) {
-            seg_ = cand;
-            dirty_ = true;
-            if ((rc = rebuild(err))) return rc;
+    auto use = [&](int seg, int cps) {
+        if (seg != seg_ || cps != cps_) {
+            seg_ = seg;
+            cps_ = cps;
+            dirty_ = true; /* new work items, and the chunk graph holds the grid */
+            return rebuild(err);
         }
-        if ((rc = launch(1, err))) return rc;
-        ECK(cudaEventRecord(ev_t0_, stream_));
-        if ((rc = launch(2, err))) return rc;
-        ECK(cudaEventRecord(ev_t1_, stream_));
-        ECK(cudaEventSynchronize(ev_t1_));
-        float ms = 0;
-        ECK(cudaEventElapsedTime(&ms, ev_t0_, ev_t1_));
-        *advanced += 3;
-        if (ms < best_ms) {
-            best_ms = ms;
-            best = cand;
+        return (int)SW2D_OK;
+    };
+    const auto cached = tuned_.find(bucket);
+    if (cached != tuned_.end()) {
+        if ((rc = use(cached->second.first, cached->second.second))) return rc;
+        bucket_ = bucket;
+        return SW2D_OK;
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    int most = 0;
+    for (int k = 0; k < T32_NCLASS; k++)
+        if (class_n_[k] > 0) most = std::max(most, bps_[k]);
+    std::pair<int, int> best(seg_, cps_);
+    float best_ms = 3.4e38f;
+    for (int seg : {64, 128, 256, 512}) {
+        for (int cps : {0, most - 1}) {
+            if (cps < 0 || (cps > 0 && most <= 1)) continue;
+            if ((rc = use(seg, cps))) return rc;
+            if ((rc = launch(1, err))) return rc;
+            ECK(cudaEventRecord(ev_t0_, stream_));
+            if ((rc = launch(2, err))) return rc;
+            ECK(cudaEventRecord(ev_t1_, stream_));
+            ECK(cudaEventSynchronize(ev_t1_));
+            float ms = 0;
+            ECK(cudaEventElapsedTime(&ms, ev_t0_, ev_t1_));
+            *advanced += 3;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = std::make_pair(seg, cps);
+            }
         }
     }
-    if (best != seg_) {
-        seg_ = best;
-        dirty_ = true;
-        if ((rc = rebuild(err))) return rc;
-    }
-    tuned_cells_ = cells;
+    if ((rc = use(best.first, best.second))) return rc;
+    tuned_[bucket] = best;
+    bucket_ = bucket;
     tuning_ms_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     tunings_++;
     return SW2D_OK;

@@ -9,6 +9,7 @@
 
 #include <nvtx3/nvToolsExt.h>
 
+#include <map>
 #include <memory>
 #include <string>
 #include <vector>
@@ -119,9 +120,13 @@ class Engine32 {
             seg_ = rows;
             dirty_ = true;
         }
-        tuned_cells_ = 0;
+        tuned_.clear();
+        bucket_ = -1;
     }
     int segment_rows() const { return seg_; }
+    /* CTAs per SM of the persistent launches (the autotuner's second
+     * choice; 0 = every CTA the SM holds) */
+    int ctas_per_sm() const { return cps_; }
     /* host milliseconds the autotuner spent timing candidates (the
      * iterations it timed were real ones: they advanced the scenarios) */
     double tuning_ms() const { return tuning_ms_; }
@@ -131,10 +136,12 @@ class Engine32 {
     int rebuild(std::string* err);
     int build_graph(std::string* err);
     int launch(int niter, std::string* err);
-    /* the autotuner: times each candidate rows-per-item on two of the
-     * scenarios' own iterations (after one untimed) and keeps the fastest;
-     * returns the iterations it advanced */
+    /* the autotuner: times each candidate pair (rows per item, CTAs per
+     * SM) on two of the scenarios' own iterations (after one untimed) and
+     * keeps the fastest, cached per size bucket (log2 of the work set's
+     * cells); returns the iterations it advanced */
     int tune(std::string* err, long long* advanced);
+    int grid_of(int k, int niter) const;
     int device_;
     int nsm_ = 0;
     int bps_[T32_NCLASS] = {};  /* CTAs per SM of each class's persistent kernel */
@@ -158,7 +165,9 @@ class Engine32 {
     long long last_iters_ = 0;
     int seg_ = 128;            /* rows per work item in use */
     int seg_fixed_ = 0;        /* set by set_segment_rows or SW2D_SEGMENT_ROWS */
-    double tuned_cells_ = 0;   /* cells of the work set the last tuning saw */
+    int cps_ = 0;              /* CTAs per SM in use (0: all that fit) */
+    int bucket_ = -1;          /* size bucket the setting in use was chosen for */
+    std::map<int, std::pair<int, int>> tuned_; /* size bucket -> (rows per item, CTAs per SM) */
     double tuning_ms_ = 0.0;
     int tunings_ = 0;
     void* pin_ = nullptr;      /* pinned staging of state downloads */

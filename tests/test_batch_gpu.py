@@ -119,10 +119,10 @@ def test_cancel_mid_run_frees_the_slot_and_leaves_the_others_unchanged():
 
 
 def test_rows_per_item_does_not_change_results():
-    """The rows per work item (the autotuner's knob) change only the work
-    split: the bed's datum tiles are fixed at 224 x 64 cells, so every
-    setting, and the tuned default, gives bit-identical results, alone and
-    in a mix."""
+    """The rows per work item and the CTAs per SM (the autotuner's knobs)
+    change only the work split: the bed's datum tiles are fixed at 224 x 64
+    cells, so every setting, and the tuned default, gives bit-identical
+    results, alone and in a mix."""
     a = scenario(300, 31, 60.0)
 
     def run(specs, rows):
@@ -140,8 +140,11 @@ def test_rows_per_item_does_not_change_results():
     assert st["rows_per_item"] == 256
     for rows, specs in ((64, [a]), (128, [scenario(500, 32, 30.0), scenario(140, 33, 90.0), a]), (512, [a]),
                         (0, [scenario(1200, 34, 20.0), a])):
-        got, _ = run(specs, rows)
+        got, st = run(specs, rows)
         assert all(np.array_equal(x, y) for x, y in zip(ref, got)), rows
+        if rows == 0:  # 1.53 M cells: the autotuner timed one size bucket
+            assert st["tunings"] == 1 and st["rows_per_item"] in (64, 128, 256, 512)
+            assert st["ctas_per_sm"] >= 0
     b = api.Batch()
     with pytest.raises(api.Sw2dError):
         b.set_rows_per_item(30)

@@ -4,6 +4,7 @@ job's time is the slowest rank's, exchanged as one scalar."""
 import os
 import socket
 
+import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
@@ -112,3 +113,34 @@ def test_cpu_baseline_falls_back_to_the_port(monkeypatch):
     monkeypatch.setattr(O, "ref_lib", lambda: None)
     v, secs, n, kind, what = bench.cpu_baseline_sample(sc, 3, 1, 2)
     assert kind == "port" and n == 3 and v > 0 and secs > 0 and "restatement" in what
+
+
+def test_fp32_only_cells_counts_leave_one_out():
+    """The conditioning check of the precision report on planted peaks: a
+    cell that only the FP32 run moves is FP32-only; a cell that one perturbed
+    run alone moves counts against that run in the leave-one-out test."""
+    import bench
+    shape = (6, 7)
+    base = np.zeros(shape)
+    res = {"fp64": {"peak": base}}
+    for k in ("fp32", "p1", "p2", "p3"):
+        res[k] = {"peak": base.copy()}
+    res["fp32"]["peak"][0, 0] = 0.005    # FP32 alone
+    res["fp32"]["peak"][1, 1] = 0.002    # FP32 and p1
+    res["p1"]["peak"][1, 1] = 0.003
+    res["p2"]["peak"][2, 2] = 0.004      # p2 alone
+    res["p3"]["peak"][3, 3] = 0.0005     # under the tolerance
+    out = bench.fp32_only_cells(res, tol=0.001)
+    assert out["cells_fp32_over_tol"] == 2 and out["cells_sensitive_union"] == 2
+    assert out["cells_fp32_only"] == 1
+    assert out["worst_fp32_only"][0] == {"row": 0, "col": 0, "err_m": 0.005, "perturbed_max_err_m": 0.0,
+                                         "peak_fp64_m": 0.0}
+    p = out["perturbations"]
+    assert p["p1"]["own_cells_unexplained_by_the_others"] == 1 and p["p1"]["own_worst_unexplained_m"] == 0.003
+    assert p["p1"]["fp32_cells_unexplained_by_the_others"] == 2
+    assert p["p2"]["own_cells_unexplained_by_the_others"] == 1 and p["p2"]["own_worst_unexplained_m"] == 0.004
+    assert p["p2"]["fp32_cells_unexplained_by_the_others"] == 1
+    assert p["p3"]["own_cells_unexplained_by_the_others"] == 0 and p["p3"]["own_worst_unexplained_m"] == 0.0
+    assert p["p3"]["fp32_worst_unexplained_m"] == 0.005
+    loo = out["leave_one_out"]
+    assert loo["perturbed_runs_max"] == 1 and loo["perturbed_worst_m_max"] == 0.004
