@@ -63,6 +63,7 @@ typedef struct sw2d_batch_stats {
     int ctas_per_sm;          /* CTAs per SM of the persistent launches (the autotuner's choice; 0 = all
                                  that fit) */
     int tunings;              /* size buckets the autotuner has timed (each is cached) */
+    double tuning_iterations; /* iterations sw2d_batch_tune advanced (in neither device_ms nor cell_updates) */
 } sw2d_batch_stats;
 
 typedef struct sw2d_batch sw2d_batch;
@@ -83,13 +84,24 @@ int sw2d_batch_poll(sw2d_batch* b, int64_t id, int* status, sw2d_ledger* ledger)
 int sw2d_batch_result(sw2d_batch* b, int64_t id, double* depth, double* qx, double* qy);
 int sw2d_batch_release(sw2d_batch* b, int64_t id);
 /* Rows per work item (a multiple of 4 in 16..512) for every scenario of the
- * batch; 0 (the default) lets the autotuner choose: when the batch's cells
- * first reach 1 M, and again when they have halved or doubled since, it
- * times 64, 128, 256 and 512 rows on three of the scenarios' own iterations
- * each and keeps the fastest.  Results do not depend on the choice (the bed's
- * datum tiles are fixed at 224 columns x 64 rows), so a scenario's results
- * are the same alone and in any mix. */
+ * batch; 0 (the default) lets the autotuner choose the work split: for a
+ * work set of at least 1 M cells it times each pair of 64, 128, 256 or 512
+ * rows per item and all or all-but-one CTAs per SM on the scenarios' own
+ * iterations (one untimed, then up to 32 in one launch, within the
+ * iterations of the sw2d_batch_step call that needs it) and keeps the
+ * fastest, cached per size bucket (log2 of the running scenarios' cells).
+ * Results do not depend on the choice (the bed's datum tiles are fixed at
+ * 224 columns x 64 rows), so a scenario's results are the same alone and in
+ * any mix. */
 int sw2d_batch_set_rows_per_item(sw2d_batch* b, int rows);
+/* Admit what fits and run the autotuner now for the running scenarios'
+ * size bucket, advancing them by at most max_iterations iterations
+ * (*iterations_out; 0 when the bucket is tuned already, rows per item are
+ * fixed, the work set is under 1 M cells or max_iterations is below 24).
+ * Finished scenarios are retired.  Lets a caller keep the tuning out of the
+ * steps it times; those iterations count in neither device_ms nor
+ * cell_updates of the stats. */
+int sw2d_batch_tune(sw2d_batch* b, int max_iterations, int* iterations_out);
 int sw2d_batch_get_stats(sw2d_batch* b, sw2d_batch_stats* out);
 const char* sw2d_batch_last_error(void);
 

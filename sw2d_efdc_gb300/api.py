@@ -74,7 +74,7 @@ class BatchStats(C.Structure):
     _fields_ = [("running", C.c_int), ("queued", C.c_int), ("work_items", C.c_int), ("rows_per_item", C.c_int),
                 ("bytes_in_use", C.c_double), ("device_ms", C.c_double), ("cell_updates", C.c_double),
                 ("launches", C.c_double), ("tuning_ms", C.c_double),
-                ("ctas_per_sm", C.c_int), ("tunings", C.c_int)]
+                ("ctas_per_sm", C.c_int), ("tunings", C.c_int), ("tuning_iterations", C.c_double)]
 
 
 REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
@@ -127,6 +127,7 @@ SIGNATURES = {
     "sw2d_batch_result": (C.c_int, [C.c_void_p, C.c_int64, _dp, _dp, _dp]),
     "sw2d_batch_release": (C.c_int, [C.c_void_p, C.c_int64]),
     "sw2d_batch_set_rows_per_item": (C.c_int, [C.c_void_p, C.c_int]),
+    "sw2d_batch_tune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "sw2d_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(BatchStats)]),
     "sw2d_batch_last_error": (C.c_char_p, []),
     "sw2d_write_efdc_concentration": (C.c_int, [C.c_char_p, C.c_char, C.c_int, C.c_int, C.c_double, C.c_int, _ip,
@@ -478,6 +479,14 @@ class Batch:
         """Rows per work item, 16..512 (0 = the autotuner's choice); results
         do not depend on it."""
         _bcheck(load().sw2d_batch_set_rows_per_item(self._h, int(rows)), "sw2d_batch_set_rows_per_item")
+
+    def tune(self, max_iterations: int = 264) -> int:
+        """Admit what fits and run the autotuner now (at most max_iterations
+        iterations of the running scenarios); returns the iterations it
+        advanced."""
+        n = C.c_int()
+        _bcheck(load().sw2d_batch_tune(self._h, int(max_iterations), C.byref(n)), "sw2d_batch_tune")
+        return n.value
 
     def stats(self) -> dict:
         st = BatchStats()

@@ -69,6 +69,7 @@ struct sw2d_batch {
     double device_ms = 0;
     double cell_updates = 0;
     long long launches = 0;
+    long long tuning_iterations = 0; /* iterations advanced by sw2d_batch_tune */
 };
 
 static sw2d::ScenarioInput to_input(const Request& r) {
@@ -241,12 +242,9 @@ int sw2d_batch_submit(sw2d_batch* b, const sw2d_scenario* s, int64_t* id_out) {
     return SW2D_OK;
 }
 
-int sw2d_batch_step(sw2d_batch* b, int iterations, int* n_running_out, int* n_queued_out) {
-    sw2d::NvtxRange r("sw2d_batch_step");
-    if (!b || iterations < 0) return bfail(SW2D_ERR_INVALID, "invalid argument");
-    if (cudaSetDevice(b->device) != cudaSuccess) return bfail(SW2D_ERR_CUDA, "cudaSetDevice");
+/* admit queued requests: first fit in arrival order */
+static void admit(sw2d_batch* b) {
     std::string err;
-    /* admit: first fit in arrival order */
     size_t in_use = b->eng->bytes_in_use();
     for (auto it = b->queue.begin(); it != b->queue.end();) {
         if (b->max_running > 0 && (int)b->running.size() >= b->max_running) break;
@@ -272,6 +270,14 @@ int sw2d_batch_step(sw2d_batch* b, int iterations, int* n_running_out, int* n_qu
         in_use += r.bytes;
         it = b->queue.erase(it);
     }
+}
+
+int sw2d_batch_step(sw2d_batch* b, int iterations, int* n_running_out, int* n_queued_out) {
+    sw2d::NvtxRange r("sw2d_batch_step");
+    if (!b || iterations < 0) return bfail(SW2D_ERR_INVALID, "invalid argument");
+    if (cudaSetDevice(b->device) != cudaSuccess) return bfail(SW2D_ERR_CUDA, "cudaSetDevice");
+    std::string err;
+    admit(b);
     if (!b->running.empty() && iterations > 0) {
         double cells = 0;
         std::vector<sw2d::Clock32> before(b->running.size());
@@ -353,6 +359,29 @@ int sw2d_batch_release(sw2d_batch* b, int64_t id) {
     return SW2D_OK;
 }
 
+int sw2d_batch_tune(sw2d_batch* b, int max_iterations, int* iterations_out) {
+    sw2d::NvtxRange r("sw2d_batch_tune");
+    if (!b || max_iterations < 0) return bfail(SW2D_ERR_INVALID, "invalid argument");
+    if (cudaSetDevice(b->device) != cudaSuccess) return bfail(SW2D_ERR_CUDA, "cudaSetDevice");
+    std::string err;
+    admit(b);
+    long long done = 0;
+    if (!b->running.empty()) {
+        int rc = b->eng->tune_now(max_iterations, &err, &done);
+        if (rc) return bfail(rc, err);
+        for (size_t k = b->running.size(); k-- > 0;) {
+            sw2d::Clock32 c;
+            if ((rc = b->eng->get_clock((int)k, &c, &err))) return bfail(rc, err);
+            if (c.done || (c.status & 3)) {
+                if ((rc = retire(b, k))) return rc;
+            }
+        }
+    }
+    b->tuning_iterations += done;
+    if (iterations_out) *iterations_out = (int)done;
+    return SW2D_OK;
+}
+
 int sw2d_batch_set_rows_per_item(sw2d_batch* b, int rows) {
     if (!b) return bfail(SW2D_ERR_INVALID, "null batch");
     if (rows != 0 && (rows < 16 || rows > sw2d::M_MAXSEG || rows % 4 != 0))
@@ -374,6 +403,7 @@ int sw2d_batch_get_stats(sw2d_batch* b, sw2d_batch_stats* out) {
     out->tuning_ms = b->eng->tuning_ms();
     out->ctas_per_sm = b->eng->ctas_per_sm();
     out->tunings = b->eng->tunings();
+    out->tuning_iterations = (double)b->tuning_iterations;
     return SW2D_OK;
 }
 

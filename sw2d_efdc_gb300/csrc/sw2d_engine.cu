@@ -507,7 +507,7 @@ int Engine32::build_graph(std::string* err) {
     return SW2D_OK;
 }
 
-int Engine32::tune(std::string* err, long long* advanced) {
+int Engine32::tune(long long budget, std::string* err, long long* advanced) {
     *advanced = 0;
     double cells = 0;
     for (auto& sp : scn_) cells += (double)sp->R * sp->C;
@@ -530,28 +530,34 @@ int Engine32::tune(std::string* err, long long* advanced) {
         bucket_ = bucket;
         return SW2D_OK;
     }
-    const auto t0 = std::chrono::steady_clock::now();
     int most = 0;
     for (int k = 0; k < T32_NCLASS; k++)
         if (class_n_[k] > 0) most = std::max(most, bps_[k]);
+    std::vector<std::pair<int, int>> cands;
+    for (int seg : {64, 128, 256, 512}) {
+        cands.emplace_back(seg, 0);
+        if (most > 1) cands.emplace_back(seg, most - 1);
+    }
+    /* iterations per candidate: one untimed (the new work split's first
+     * launch), then one timed launch of up to a chunk */
+    const long long per = std::min<long long>(kChunk + 1, budget / (long long)cands.size());
+    if (per < 3) return SW2D_OK; /* too few iterations to tune now: a later, longer call will */
+    const auto t0 = std::chrono::steady_clock::now();
     std::pair<int, int> best(seg_, cps_);
     float best_ms = 3.4e38f;
-    for (int seg : {64, 128, 256, 512}) {
-        for (int cps : {0, most - 1}) {
-            if (cps < 0 || (cps > 0 && most <= 1)) continue;
-            if ((rc = use(seg, cps))) return rc;
-            if ((rc = launch(1, err))) return rc;
-            ECK(cudaEventRecord(ev_t0_, stream_));
-            if ((rc = launch(2, err))) return rc;
-            ECK(cudaEventRecord(ev_t1_, stream_));
-            ECK(cudaEventSynchronize(ev_t1_));
-            float ms = 0;
-            ECK(cudaEventElapsedTime(&ms, ev_t0_, ev_t1_));
-            *advanced += 3;
-            if (ms < best_ms) {
-                best_ms = ms;
-                best = std::make_pair(seg, cps);
-            }
+    for (const auto& cand : cands) {
+        if ((rc = use(cand.first, cand.second))) return rc;
+        if ((rc = launch(1, err))) return rc;
+        ECK(cudaEventRecord(ev_t0_, stream_));
+        if ((rc = launch((int)(per - 1), err))) return rc;
+        ECK(cudaEventRecord(ev_t1_, stream_));
+        ECK(cudaEventSynchronize(ev_t1_));
+        float ms = 0;
+        ECK(cudaEventElapsedTime(&ms, ev_t0_, ev_t1_));
+        *advanced += per;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = cand;
         }
     }
     if ((rc = use(best.first, best.second))) return rc;
@@ -560,6 +566,15 @@ int Engine32::tune(std::string* err, long long* advanced) {
     tuning_ms_ += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     tunings_++;
     return SW2D_OK;
+}
+
+int Engine32::tune_now(long long budget, std::string* err, long long* advanced) {
+    ECK(cudaSetDevice(device_));
+    *advanced = 0;
+    int rc = rebuild(err);
+    if (rc) return rc;
+    if (scn_.empty() || budget <= 0) return SW2D_OK;
+    return tune(budget, err, advanced);
 }
 
 int Engine32::set_t_end(int index, double t_end, std::string* err) {
@@ -586,9 +601,7 @@ int Engine32::run(long long n, std::string* err) {
     if (scn_.empty() || n <= 0) return SW2D_OK;
     ECK(cudaEventRecord(ev_a_, stream_));
     long long done = 0;
-    if (n >= 16) {
-        if ((rc = tune(err, &done))) return rc;
-    }
+    if ((rc = tune(n, err, &done))) return rc;
     if ((rc = build_graph(err))) return rc;
     for (; n - done >= kChunk; done += kChunk) {
         if (graph_)

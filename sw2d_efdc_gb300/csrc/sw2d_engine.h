@@ -131,16 +131,21 @@ class Engine32 {
      * iterations it timed were real ones: they advanced the scenarios) */
     double tuning_ms() const { return tuning_ms_; }
     int tunings() const { return tunings_; }
+    /* the autotuner now, for the work set's size bucket, advancing the
+     * scenarios by at most `budget` iterations (*advanced of them; 0 when
+     * the bucket is tuned already or the budget holds too few) */
+    int tune_now(long long budget, std::string* err, long long* advanced);
 
   private:
     int rebuild(std::string* err);
     int build_graph(std::string* err);
     int launch(int niter, std::string* err);
     /* the autotuner: times each candidate pair (rows per item, CTAs per
-     * SM) on two of the scenarios' own iterations (after one untimed) and
-     * keeps the fastest, cached per size bucket (log2 of the work set's
-     * cells); returns the iterations it advanced */
-    int tune(std::string* err, long long* advanced);
+     * SM) on the scenarios' own iterations -- one untimed, then up to a
+     * chunk's worth in one persistent launch, as the chunks run -- and keeps
+     * the fastest, cached per size bucket (log2 of the work set's cells).
+     * Advances at most `budget` iterations and returns how many. */
+    int tune(long long budget, std::string* err, long long* advanced);
     int grid_of(int k, int niter) const;
     int device_;
     int nsm_ = 0;

@@ -68,9 +68,6 @@ struct SmemM {
     unsigned q;                 /* queue ticket of the item in hand (~0u: leave) */
     unsigned qn;                /* the ticket drawn ahead for the next item */
     int last;                   /* this CTA finished its scenario's iteration */
-    unsigned done[NS];          /* warps that finished a block of each stage, counted modulo NW */
-    unsigned lastiss[NS];       /* the CTA's block count of the latest block loaded into each stage */
-    int stop;                   /* a warp's staging wait ran out: every warp leaves the item */
     ClsStage cls[NS];
     RwStage rw[NS];
 };
@@ -100,15 +97,6 @@ __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned coun
 __device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
-}
-
-/* returns the old value; acquire-release at CTA scope, so that the warps'
- * shared-memory reads of a stage come before the refill that the last of
- * them issues */
-__device__ __forceinline__ unsigned atom_add_acqrel_cta(unsigned* p, unsigned v) {
-    unsigned old;
-    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;" : "=r"(old) : "r"(smem_addr(p)), "r"(v) : "memory");
-    return old;
 }
 
 __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
@@ -380,10 +368,7 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
     if (tid == 0 && !P.stall_staging) {
         /* the staging buffers were last read by the generic proxy */
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (int b = 0; b < NS && b < nblk; b++) {
-            issue(b, (int)((gb + b) % NS));
-            S.lastiss[(gb + b) % NS] = gb + b;
-        }
+        for (int b = 0; b < NS && b < nblk; b++) issue(b, (int)((gb + b) % NS));
     }
 
     /* lane geometry: staged columns sc, sc+1; global columns cg, cg+1 */
@@ -442,25 +427,38 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
         return v;
     };
 
-    bool stopped = false;
     for (int b = 0; b < nblk; b++) {
         const int st = (int)((gb + b) % NS);
-        /* bounded wait for the block (about 2^31 cycles), or until another
-         * warp of the CTA has given up; no CTA barrier per block, so the
-         * warps drift apart by up to a block */
+        /* bounded wait for the block (about 2^31 cycles); the CTA agrees on
+         * the outcome so that no warp is left waiting at a barrier */
         {
             const unsigned par = ((gb + b) / NS) & 1u;
-            bool ok = mbar_try_wait(&S.bar[st], par);
-            if (!ok) {
-                const long long t0 = clock64();
-                while (!(ok = mbar_try_wait(&S.bar[st], par))) {
-                    if (*reinterpret_cast<volatile int*>(&S.stop) || clock64() - t0 > (1ll << 31)) break;
+            long long t0 = clock64();
+            bool ok = true;
+            while (!mbar_try_wait(&S.bar[st], par)) {
+                if (clock64() - t0 > (1ll << 31)) {
+                    ok = false;
+                    break;
                 }
             }
-            if (__any_sync(0xffffffffu, !ok)) {
-                if (lane == 0) *reinterpret_cast<volatile int*>(&S.stop) = 1;
-                stopped = true;
-                break;
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicOr(&clk->status, 2);
+                    /* Blocks b .. b+NS-1 were issued (none under the staging
+                     * stall of the failure test) and their loads may still
+                     * be in flight into this CTA's shared memory: wait for
+                     * them, again bounded, before the CTA exits and its
+                     * shared memory is handed to another CTA.  The launch's
+                     * results are void either way (status bit 1). */
+                    const int issued = P.stall_staging ? 0 : min(nblk, b + NS);
+                    for (int bb = b; bb < issued; bb++) {
+                        const long long t1 = clock64();
+                        while (!mbar_try_wait(&S.bar[(gb + bb) % NS], ((gb + bb) / NS) & 1u) &&
+                               clock64() - t1 <= (1ll << 31)) {
+                        }
+                    }
+                }
+                return false;
             }
         }
         const float* sh = &S.stage[st][0][0][0];
@@ -670,35 +668,11 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
                 }
             }
         }
-        /* the last warp to finish with block b refills its stage with
-         * block b + NS */
-        __syncwarp();
-        if (lane == 0) {
-            const unsigned prev = atom_add_acqrel_cta(&S.done[st], 1u);
-            if (prev % NW == NW - 1 && b + NS < nblk) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue(b + NS, st);
-                S.lastiss[st] = gb + b + NS;
-            }
+        __syncthreads(); /* every warp is done with block b */
+        if (tid == 0 && b + NS < nblk) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(b + NS, st);
         }
-    }
-    if (__syncthreads_or(stopped)) {
-        if (tid == 0) {
-            atomicOr(&clk->status, 2);
-            /* The latest block loaded into each stage may still be in flight
-             * into this CTA's shared memory: wait for it, again bounded,
-             * before the CTA exits and its shared memory is handed to
-             * another CTA.  The launch's results are void either way
-             * (status bit 1). */
-            for (int k = 0; k < NS; k++) {
-                const unsigned bb = S.lastiss[k];
-                if (bb == ~0u) continue;
-                const long long t1 = clock64();
-                while (!mbar_try_wait(&S.bar[k], (bb / NS) & 1u) && clock64() - t1 <= (1ll << 31)) {
-                }
-            }
-        }
-        return false;
     }
     gb += (unsigned)nblk;
 
@@ -970,12 +944,7 @@ __global__ void __launch_bounds__(NT, 4) k32_persist(const Scn32* __restrict__ s
     extern __shared__ __align__(128) unsigned char smem_raw[];
     SmemM& S = *reinterpret_cast<SmemM*>(smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u));
     if (threadIdx.x == 0) {
-        for (int k = 0; k < NS; k++) {
-            mbar_init(&S.bar[k], 1);
-            S.done[k] = 0u;
-            S.lastiss[k] = ~0u;
-        }
-        S.stop = 0;
+        for (int k = 0; k < NS; k++) mbar_init(&S.bar[k], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();

@@ -153,6 +153,39 @@ def test_rows_per_item_does_not_change_results():
     b.close()
 
 
+def test_explicit_tuning_runs_once_per_size_bucket():
+    """sw2d_batch_tune times every candidate work split on the scenarios' own
+    iterations before any step (so a caller keeps it out of the steps it
+    times), caches the choice for the size bucket, counts its iterations in
+    neither the device time nor the cell-updates, and leaves the results
+    bit-identical to a fixed split."""
+    specs = [scenario(1100, 51, 40.0), scenario(300, 52, 60.0)]
+    b = api.Batch()
+    b.set_rows_per_item(256)
+    ids = [b.submit(**s) for s in specs]
+    assert b.tune(264) == 0  # rows per item fixed: nothing to tune
+    while b.step(32) != (0, 0):
+        pass
+    ref = [b.result(i) for i in ids]
+    b.close()
+    b = api.Batch()
+    ids = [b.submit(**s) for s in specs]
+    assert b.tune(11) == 0  # too few iterations: fewer than three per candidate
+    n = b.tune(264)
+    assert n == 264  # eight candidates (four CTAs per SM fit) x (1 untimed + 32 timed)
+    assert b.tune(264) == 0  # the bucket is cached
+    st = b.stats()
+    assert st["tunings"] == 1 and st["tuning_iterations"] == n
+    assert st["device_ms"] == 0.0 and st["cell_updates"] == 0.0
+    assert st["rows_per_item"] in (64, 128, 256, 512) and st["ctas_per_sm"] >= 0
+    while b.step(32) != (0, 0):
+        pass
+    got = [b.result(i) for i in ids]
+    b.close()
+    for x, y in zip(ref, got):
+        assert all(np.array_equal(p, q) for p, q in zip(x, y))
+
+
 def test_request_submitted_while_others_run_matches_alone():
     """Continuous batching: a request that arrives while other requests are
     already advancing on the GPU joins at the next step and finishes
