@@ -651,21 +651,24 @@ __device__ __forceinline__ bool march_item(SmemM& S, const Scn32& P, const int4 
             };
             if (r >= rs && r < re) {
                 const int dc = DRY[s3], dN = DRY[s0], dS = DRY[s2];
+                float2 fN = FX[s3], fS = FX[s2], fW = FY[s3], fE = FYR[s3];
                 if (__any_sync(0xffffffffu, (dc | dN | dS) != 0)) {
-                    /* treat_error (SW2D-EFDC.cu:695-725): no outflow from a dry
-                     * cell.  The whole finish is repeated in both branches so
-                     * that the rare clipping stays a real branch. */
+                    /* treat_error (SW2D-EFDC.cu:695-725): no outflow from a
+                     * dry cell; a warp-uniform branch taken only near dry
+                     * cells, the finish below shared by both paths (one
+                     * copy of it per row keeps the unrolled loop small) */
                     const int dW = leftbits(dc), dE = rightbits(dc);
                     const B2 bc = bits2(dc), bN = bits2(dN), bS = bits2(dS), bW = bits2(dW), bE = bits2(dE);
-                    const float2 fN = FX[s3], fS = FX[s2], fW = FY[s3], fE = FYR[s3];
                     const B2 zN = (gt2(fN, 0.f) & bN) | (lt2(fN, 0.f) & bc);
                     const B2 zS = (gt2(fS, 0.f) & bc) | (lt2(fS, 0.f) & bS);
                     const B2 zW = (gt2(fW, 0.f) & bW) | (lt2(fW, 0.f) & bc);
                     const B2 zE = (gt2(fE, 0.f) & bc) | (lt2(fE, 0.f) & bE);
-                    finish(sel2(zN, f2(0.f), fN), sel2(zS, f2(0.f), fS), sel2(zW, f2(0.f), fW), sel2(zE, f2(0.f), fE));
-                } else {
-                    finish(FX[s3], FX[s2], FY[s3], FYR[s3]);
+                    fN = sel2(zN, f2(0.f), fN);
+                    fS = sel2(zS, f2(0.f), fS);
+                    fW = sel2(zW, f2(0.f), fW);
+                    fE = sel2(zE, f2(0.f), fE);
                 }
+                finish(fN, fS, fW, fE);
             }
         }
         __syncthreads(); /* every warp is done with block b */
