@@ -41,10 +41,10 @@ BYTES_PER_CELL_K64_FLUX = 66
 # dram__bytes_read.sum + dram__bytes_write.sum = 821.7 + 250.3 MB over 16.78 M cells
 TRAFFIC_PER_CELL_K64_FLUX = 63.90
 BYTES_PER_CELL_FP32_CFG3 = 37  # h,qx,qy r+w 24 + z offset 4 + info byte 1 + Kahan compensation r+w 8
-# DRAM bytes per cell-update of the FP32 step (k32_march, the per-iteration kernel before the persistent one), 4096 x 4096 precision form at t = 1200 s: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum = 360.3 + 221.8 MB over 16.78 M cells; the
-# launch streams every field once, so the figure scales with cells
-TRAFFIC_PER_CELL_K32_MARCH = 34.69
+# DRAM bytes per cell-update of the FP32 step (k32_persist), 4096 x 4096 precision form at t = 1200 s,
+# one launch of four iterations: ncu dram__bytes_read.sum + dram__bytes_write.sum = 1419.1 + 1031.9 MB
+# over 4 x 16.78 M cell-updates; every field is streamed once per iteration, so the figure scales with cells
+TRAFFIC_PER_CELL_K32 = 36.52
 
 
 class TimedRegion:
@@ -279,8 +279,8 @@ def run_fp32_leg(args, peak):
         "roofline": {"bound": "hbm", "kernel": "k32_persist",
                      "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "bytes_per_cell_update": BYTES_PER_CELL_FP32_CFG3,
-                     "traffic": round(TRAFFIC_PER_CELL_K32_MARCH * cells / 1e9, 4),
-                     "traffic_unit": "GB per launch (ncu at 4096x4096, scaled by cells)"},
+                     "traffic": round(TRAFFIC_PER_CELL_K32 * cells / 1e9, 4),
+                     "traffic_unit": "GB per iteration (ncu at 4096x4096, scaled by cells)"},
         "balance_error": led["balance_error"],
         "vs_fp64_plain": None,
     }

@@ -7,7 +7,9 @@
   non-negative and zero on inactive cells, and a restored snapshot continues
   bit for bit.
 * FP32 precision form, 8192 x 8192: volume balance within 1e-6 of the
-  inflow, and two handles of the same inputs agree bit for bit.
+  inflow, two handles of the same inputs agree bit for bit, and the depths
+  stay within 1 mm of the FP64 path's (p99.9) over the storm's first
+  twenty minutes.
 """
 import os
 
@@ -76,11 +78,9 @@ def test_fp64_full_raster_wet_regime_properties(pondbreak):
     m.close()
 
 
-def test_fp32_full_raster_balance_and_reproducibility(monkeypatch):
-    # the rows per work item fixed: the autotuner's timed choice may differ
-    # between two engines, and the tile datum (hence binary32 rounding of the
-    # bed) follows the work items
-    monkeypatch.setenv("SW2D_SEGMENT_ROWS", "256")
+def test_fp32_full_raster_balance_and_reproducibility():
+    # the autotuner may choose another work split for each handle; the bed's
+    # datum tiles are fixed, so the results may not differ
     sc = synth.config3(8192, 8192)
     ms = [_model(sc, api.FP32) for _ in range(2)]
     for m in ms:
@@ -90,3 +90,29 @@ def test_fp32_full_raster_balance_and_reproducibility(monkeypatch):
     assert np.array_equal(ms[0].depth(), ms[1].depth())
     for m in ms:
         m.close()
+
+
+def test_fp32_against_fp64_at_full_size():
+    """The FP32 form against the FP64 path (bit-identical to the oracle) on
+    the full 8192 x 8192 raster of the precision workload, both from the dry
+    start to t = 1200 s (the storm's first twenty minutes): depth error p99.9
+    within 1 mm, no more than 0.1 % of the cells above 1 mm, and both volume
+    balances within their bounds.  (The full 3 h comparison, with the
+    perturbed FP64 runs that show which cells are ill-conditioned, is the
+    benchmark's precision report.)"""
+    sc = synth.config3(8192, 8192)
+    out = {}
+    for prec in (api.FP64, api.FP32):
+        m = _model(sc, prec)
+        m.advance(1200.0)
+        out[prec] = (m.depth(), m.ledger())
+        m.close()
+    (h64, l64), (h32, l32) = out[api.FP64], out[api.FP32]
+    assert l64["time"] == l32["time"] == 1200.0
+    assert abs(l64["balance_error"]) < 1e-12 and abs(l32["balance_error"]) < 1e-6
+    err = np.abs(h32 - h64)
+    p999 = float(np.percentile(err, 99.9))
+    over = int((err > 1e-3).sum())
+    print("8192^2 FP32 vs FP64 at 1200 s: max %.3g m, p99.9 %.3g m, cells over 1 mm %d of %d, max depth %.3f m"
+          % (err.max(), p999, over, err.size, h64.max()))
+    assert p999 <= 1e-3 and over <= 1e-3 * err.size
