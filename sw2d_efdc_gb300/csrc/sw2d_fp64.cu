@@ -243,7 +243,12 @@ __device__ __forceinline__ double face_speed(double vel, double hm, double g, do
 __device__ __forceinline__ unsigned long long block_face_speed_max(bool ok, double vel, double hm, double g,
                                                                    double rd, float* smf,
                                                                    unsigned long long* smu) {
-    const float s32 = ok ? (fabsf((float)vel) + sqrtf((float)g * (float)hm)) * (float)rd : 0.0f;
+    /* binary32 estimates by integer operations: a conversion from binary64
+     * costs a binary64 operation on this GPU */
+    const float s32 = ok ? (fabsf(sw2d_f32_est_of_f64(vel)) +
+                            sqrtf(sw2d_f32_est_of_f64(g) * sw2d_f32_est_of_f64(hm))) *
+                               sw2d_f32_est_of_f64(rd)
+                         : 0.0f;
     const float m32 = block_max_f32_all(s32, smf);
     unsigned long long bits = 0ull;
     if (ok && s32 >= m32 * 0.99999f) bits = (unsigned long long)__double_as_longlong(face_speed(vel, hm, g, rd));
@@ -385,7 +390,7 @@ __device__ __forceinline__ double continuity(const StepParams& p, size_t i, uint
         pct = p.pct_land;
         evapo = 0.000;
     }
-    const double rcell = p.rainw ? rr * (double)p.rainw[i] : rr;
+    const double rcell = p.rainw ? rr * sw2d_f64_of_f32(p.rainw[i]) : rr; /* exact, off the FP64 pipe */
     /* (((dqx/dx + dqy/dy) - q_src) - r pct) + e; subtracting a zero source
      * and adding a zero evaporation change no value, so they are skipped */
     double sum = div_spacing(divx, p.dx, p.rdx, p.kdx) + div_spacing(divy, p.dy, p.rdy, p.kdy);

@@ -160,6 +160,52 @@ SW2D_HD int sw2d_le_pos(double x, double t) { return (int64_t)sw2d_f64_bits(x) <
 SW2D_HD double sw2d_fma(double a, double b, double c) { return fma(a, b, c); }
 SW2D_HD float sw2d_fmaf(float a, float b, float c) { return fmaf(a, b, c); }
 
+/* ---- conversions between binary32 and binary64 on the integer pipes ----
+ * On GB300 a conversion between binary32 and binary64, or between a 64-bit
+ * integer and binary32, runs on the FP64 pipe at the binary64 rate (a
+ * micro-benchmark: about one binary64 addition each).  These build the
+ * result from the bit pattern instead. */
+
+/* (double)f, exact: normal and zero operands by integer operations (the
+ * rest, subnormal, infinite or NaN, through the hardware conversion) */
+SW2D_HD double sw2d_f64_of_f32(float f) {
+    const uint32_t b = sw2d_f32_bits(f);
+    const uint32_t e = (b >> 23) & 0xffu;
+    const uint64_t sign = (uint64_t)(b & 0x80000000u) << 32;
+    if (e - 1u < 0xfeu)
+        return sw2d_f64_from_bits(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7fffffu) << 29));
+    if ((b & 0x7fffffffu) == 0u) return sw2d_f64_from_bits(sign);
+    return (double)f;
+}
+
+/* an estimate of (float)x for the binary32 prefilters: the significand
+ * truncated to 24 bits (relative error below 2^-23); magnitudes below the
+ * binary32 normal range give 0, above it the hardware conversion */
+SW2D_HD float sw2d_f32_est_of_f64(double x) {
+    const uint64_t b = sw2d_f64_bits(x);
+    const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    if (e - 897u < 254u)
+        return sw2d_f32_from_bits((hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+    if (e < 897u) return 0.0f;
+    return (float)x;
+}
+
+/* an estimate of (float)v for a 32-bit unsigned v (relative error below
+ * 2^-22): v = hi 2^16 + lo, each half exact in binary32 by the 2^23
+ * magic-number construction */
+SW2D_HD float sw2d_f32_est_of_u32(uint32_t v) {
+    const float h = sw2d_f32_from_bits(0x4b000000u | (v >> 16)) - 8388608.0f;
+    const float l = sw2d_f32_from_bits(0x4b000000u | (v & 0xffffu)) - 8388608.0f;
+    return sw2d_fmaf(h, 65536.0f, l);
+}
+
+/* nearest integer to x for |x| < 2^22, by the 1.5 2^23 magic number */
+SW2D_HD int32_t sw2d_i32_near_f32(float x) {
+    return (int32_t)(sw2d_f32_bits(x + 12582912.0f) - 0x4b400000u);
+}
+
+
 /* a / d for a constant divisor d with rd = RN(1/d): one product and one
  * fma-based residual correction (Markstein's theorem: with rd = RN(1/d) the
  * corrected quotient is the correctly rounded a/d). */
@@ -272,7 +318,7 @@ SW2D_HD double sw2d_rpow_manning(double x) {
     const float ph = w0h * s;
     const float pl = sw2d_fmaf(w0h, s, -ph);
     const float rest = pl + w0l + w0h * ul + w0l * s;
-    return (double)w0h + ((double)ph + (double)rest);
+    return sw2d_f64_of_f32(w0h) + (sw2d_f64_of_f32(ph) + sw2d_f64_of_f32(rest));
 }
 
 /* ------------------------------------------------------------------------
@@ -301,7 +347,11 @@ SW2D_HD float sw2d_rcp_est(float x) {
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 #else
+#if defined(SW2D_TEST_EST_SCALE) /* tests: a seed as far off as the hardware approximation may be */
+    return (1.0f / x) * (float)(SW2D_TEST_EST_SCALE);
+#else
     return 1.0f / x;
+#endif
 #endif
 }
 
@@ -378,7 +428,11 @@ SW2D_HD float sw2d_sqrt_est(float x) {
     asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
     return r;
 #else
+#if defined(SW2D_TEST_EST_SCALE)
+    return sqrtf(x) * (float)(SW2D_TEST_EST_SCALE);
+#else
     return sqrtf(x);
+#endif
 #endif
 }
 
@@ -401,20 +455,34 @@ SW2D_HD double sw2d_sqrt_rn(double x) {
     const float sh = sw2d_sqrt_est(fh);
     const float d = sw2d_fmaf(-sh, sh, fh) + fl;      /* f - sh^2 */
     const float corr = d * (0.5f * sw2d_rcp_est(sh)); /* Newton: sqrt(f) ~ sh + d / (2 sh) */
-    /* S0 = (sh + corr) 2^54: sh has 24 significant bits, so sh 2^54 is an integer */
+    /* S0 = (sh + corr) 2^54: sh has 24 significant bits, so sh 2^54 is an
+     * integer; corr 2^54 (|corr| < 2^-16 for any seed within 2^-17 of
+     * sqrt(fh)) is taken to the nearest integer as 2^16 hi + lo, both in 32
+     * bits */
     const uint32_t sb = sw2d_f32_bits(sh);
     const int se = (int)(sb >> 23) - 127; /* sh in [1, 2): se = 0 (or 1 when sh rounds to 2) */
     const uint64_t s_int = ((uint64_t)((sb & 0x7fffffu) | 0x800000u)) << (31 + se);
-    uint64_t S = s_int + (uint64_t)(int64_t)(corr * 18014398509481984.0f); /* corr 2^54 */
+    const float c = corr * 18014398509481984.0f; /* corr 2^54, |c| < 2^38 */
+    const int32_t chi = sw2d_i32_near_f32(c * 1.52587890625e-05f);
+    const int32_t clo = sw2d_i32_near_f32(sw2d_fmaf((float)chi, -65536.0f, c));
+    uint64_t S = s_int + (uint64_t)((int64_t)chi * 65536 + clo);
     /* exact remainder N - S^2 in 128 bits, N = m 2^56 */
     const uint64_t nh = m >> 8, nl = m << 56;
     const uint64_t sl = S * S, sh2 = sw2d_umulhi(S, S);
     const uint64_t rl = nl - sl;
     const uint64_t rh = nh - sh2 - (nl < sl ? 1ull : 0ull);
-    /* r / 2^8 fits in a signed 64-bit number (|r| < 2^70) */
-    const int64_t r8 = (int64_t)((rh << 56) | (rl >> 8));
-    const float dl = (float)r8 * 256.0f * (0.5f * sw2d_rcp_est((float)S));
-    S += (uint64_t)(int64_t)dl;
+    /* r / 2^16 fits in a signed 64-bit number (|r| < 2^79: S0 within 2^22
+     * units); its estimate in binary32 from its two 32-bit halves, and
+     * 1 / (2 S) from S's top 32 bits (S < 2^56); the correction
+     * dl = r / (2 S) is below 2^22 */
+    const int64_t r16 = (int64_t)((rh << 48) | (rl >> 16));
+    const uint64_t ar = r16 < 0 ? (uint64_t)0 - (uint64_t)r16 : (uint64_t)r16;
+    const float rf = sw2d_fmaf(sw2d_f32_est_of_u32((uint32_t)(ar >> 32)), 4294967296.0f,
+                               sw2d_f32_est_of_u32((uint32_t)ar));
+    const float sf = sw2d_f32_est_of_u32((uint32_t)(S >> 24)) * 16777216.0f;
+    const float dl = rf * 65536.0f * (0.5f * sw2d_rcp_est(sf));
+    const int64_t di = (int64_t)sw2d_i32_near_f32(dl);
+    S += (uint64_t)(r16 < 0 ? -di : di);
     int64_t r = (int64_t)((m << 56) - S * S); /* exact: |N - S^2| < 2^60 now */
     while (r < 0) {
         S--;

@@ -16,6 +16,10 @@ void rpow(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i
 void divc(const double* a, double d, double* y, long n) { double r = 1.0 / d; for (long i = 0; i < n; i++) y[i] = sw2d_div_const(a[i], d, r); }
 void sqrtrn(const double* a, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_sqrt_rn(a[i]); }
 void divrn(const double* a, const double* b, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_div_rn(a[i], b[i]); }
+void f64of32(const float* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_f64_of_f32(x[i]); }
+void f32est(const double* x, float* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_f32_est_of_f64(x[i]); }
+void u32est(const unsigned* v, float* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_f32_est_of_u32(v[i]); }
+void i32near(const float* x, int* y, long n) { for (long i = 0; i < n; i++) y[i] = sw2d_i32_near_f32(x[i]); }
 void lnf(const double* x, double* y, long n) { for (long i = 0; i < n; i++) y[i] = (double)sw2d_ln_f32(x[i]); }
 void scal(const double* x, double* h, double* q, double* m0, long n) {
     for (long i = 0; i < n; i++) {
@@ -34,16 +38,19 @@ void cmps(const double* a, const double* b, int* out, long n) {
 """
 
 
-@pytest.fixture(scope="module")
-def mathlib(tmp_path_factory):
-    d = tmp_path_factory.mktemp("m")
+def _build_mathlib(d, defines=()):
     src = d / "m.c"
     src.write_text(SRC)
     so = d / "m.so"
-    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I",
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", *defines, "-I",
                            os.path.join(ROOT, "sw2d_efdc_gb300", "csrc"), str(src), "-o", str(so), "-lm"])
     L = ctypes.CDLL(str(so))
     dp = ctypes.POINTER(ctypes.c_double)
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.f64of32.argtypes = [fp, dp, ctypes.c_long]
+    L.f32est.argtypes = [dp, fp, ctypes.c_long]
+    L.u32est.argtypes = [ctypes.POINTER(ctypes.c_uint32), fp, ctypes.c_long]
+    L.i32near.argtypes = [fp, ctypes.POINTER(ctypes.c_int32), ctypes.c_long]
     L.rpow.argtypes = [dp, dp, ctypes.c_long]
     L.divc.argtypes = [dp, ctypes.c_double, dp, ctypes.c_long]
     L.lnf.argtypes = [dp, dp, ctypes.c_long]
@@ -53,6 +60,11 @@ def mathlib(tmp_path_factory):
     L.cmps.argtypes = [dp, dp, ctypes.POINTER(ctypes.c_int), ctypes.c_long]
     L.cmpp.argtypes = [dp, ctypes.c_double, ctypes.POINTER(ctypes.c_int), ctypes.c_long]
     return L, dp
+
+
+@pytest.fixture(scope="module")
+def mathlib(tmp_path_factory):
+    return _build_mathlib(tmp_path_factory.mktemp("m"))
 
 
 def _all_classes(rng, n):
@@ -228,3 +240,71 @@ def test_integer_square_root_is_the_ieee_square_root(mathlib):
         ref = np.sqrt(a)
     same = (y.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(y) & np.isnan(ref))
     assert same.all(), (a[~same][:3], y[~same][:3], ref[~same][:3])
+
+
+def test_conversions_on_the_integer_pipes(mathlib):
+    """The binary32 <-> binary64 conversions built from bit patterns: the
+    exact widening equals the C conversion for every class of binary32; the
+    narrowing estimate is within 2^-23 relative (0 below the binary32 normal
+    range); the 32-bit unsigned estimate within 2^-22; the nearest-integer
+    construction exact for |x| < 2^22."""
+    L, dp = mathlib
+    fp = ctypes.POINTER(ctypes.c_float)
+    rng = np.random.default_rng(9)
+    bits = rng.integers(0, 1 << 32, 1_000_000, dtype=np.uint64).astype(np.uint32)
+    f = bits.view(np.float32).copy()
+    f[:8] = [0.0, -0.0, np.inf, -np.inf, 1e-45, -1e-45, 1.1754944e-38, 3.4028235e38]
+    f = f[~np.isnan(f)]
+    y = np.empty(f.size)
+    L.f64of32(f.ctypes.data_as(fp), y.ctypes.data_as(dp), f.size)
+    assert np.array_equal(y.view(np.uint64), f.astype(np.float64).view(np.uint64))
+    x = _all_classes(rng, 500_000)
+    x = x[np.isfinite(x)]
+    e = np.empty(x.size, np.float32)
+    L.f32est(x.ctypes.data_as(dp), e.ctypes.data_as(fp), x.size)
+    small = np.abs(x) < np.finfo(np.float32).tiny
+    big = np.abs(x) > np.finfo(np.float32).max
+    assert (e[small] == 0).all()
+    with np.errstate(over="ignore"):
+        assert np.array_equal(e[big], x[big].astype(np.float32))  # the hardware conversion: infinity
+    mid = ~small & ~big
+    rel = np.abs(e[mid].astype(np.float64) - x[mid]) / np.abs(x[mid])
+    assert rel.max() < 2.0 ** -23 and (np.sign(e[mid]) == np.sign(x[mid])).all()
+    v = rng.integers(0, 1 << 32, 1_000_000, dtype=np.uint64).astype(np.uint32)
+    v[:4] = [0, 1, 0xFFFFFFFF, 1 << 31]
+    u = np.empty(v.size, np.float32)
+    L.u32est(v.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), u.ctypes.data_as(fp), v.size)
+    vv = v.astype(np.float64)
+    assert (np.abs(u - vv) <= 2.0 ** -22 * vv).all()
+    z = (rng.random(1_000_000) - 0.5).astype(np.float32) * np.float32(2 ** 23 - 4)
+    z[:4] = [0.0, -0.5, 0.5, 4194303.0]
+    k = np.empty(z.size, np.int32)
+    L.i32near(z.ctypes.data_as(fp), k.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), z.size)
+    assert np.array_equal(k, np.rint(z).astype(np.int32))
+
+
+@pytest.mark.parametrize("scale", ["(1.0f+16*1.1920929e-7f)", "(1.0f-16*1.1920929e-7f)"])
+def test_integer_division_and_square_root_with_coarse_seeds(tmp_path, scale):
+    """The correctly rounded division and square root do not depend on how
+    good their binary32 seeds are: with every reciprocal and square-root
+    seed off by 16 units in the last place (far more than the hardware
+    approximations the GPU uses), both still return the IEEE result bit for
+    bit."""
+    L, dp = _build_mathlib(tmp_path, ["-DSW2D_TEST_EST_SCALE=" + scale])
+    rng = np.random.default_rng(12)
+    a = _all_classes(rng, 400_000)
+    b = _all_classes(rng, 400_000)
+    n = min(a.size, b.size)
+    a, b = np.ascontiguousarray(a[:n]), np.ascontiguousarray(b[:n])
+    k = n // 4
+    a[:k] = np.abs(rng.standard_normal(k)) * 10.0 ** rng.uniform(-8, 3, k)
+    b[:k] = 10.0 ** rng.uniform(-4, 1, k)
+    y = np.empty(n)
+    L.divrn(a.ctypes.data_as(dp), b.ctypes.data_as(dp), y.ctypes.data_as(dp), n)
+    with np.errstate(all="ignore"):
+        ref = a / b
+    assert ((y.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(y) & np.isnan(ref))).all()
+    L.sqrtrn(a.ctypes.data_as(dp), y.ctypes.data_as(dp), n)
+    with np.errstate(all="ignore"):
+        ref = np.sqrt(a)
+    assert ((y.view(np.uint64) == ref.view(np.uint64)) | (np.isnan(y) & np.isnan(ref))).all()
