@@ -544,6 +544,21 @@ def run_batched_leg(args, peak, fp64_value):
             "input_generation_s": round(gen_s, 1)}
 
 
+def make_served_specs(n, seed, t_scale=1.0):
+    """Requests of the served form: side log-uniform in [256, 4096], the
+    precision workload's generator (plane + bumps, n 0.03, gamma 5-min
+    hyetograph mean 20 mm/h), duration U(0.5, 6) h scaled by t_scale."""
+    from sw2d_efdc_gb300 import api, synth
+    rng = np.random.default_rng(seed)
+    sides = synth.loguniform_sides(n, 256, 4096, rng)
+    specs = []
+    for side in sides:
+        sc = synth.served_request(int(side), rng)
+        specs.append(dict(dem=sc.dem, manning=sc.manning, rain_mm=sc.rain_mm, dtrain=sc.dtrain, dx=sc.dx,
+                          t_end=sc.t_end * t_scale, outflow=api.OUTFLOW_SOUTH, cfl=sc.cfl, dt_max=sc.dt_max))
+    return specs
+
+
 def run_served_leg(args, fp64_value):
     """The served form: a finite Poisson trace of requests (lambda 20/s, side
     log-uniform 256-4096) admitted against an HBM budget as they arrive and
@@ -553,7 +568,7 @@ def run_served_leg(args, fp64_value):
     n = args.serve_n
     arrivals = synth.poisson_arrivals(n, 20.0, rng)
     t0 = time.time()
-    specs = make_batch_specs(n, 256, 4096, 6, t_scale=args.serve_time_scale)
+    specs = make_served_specs(n, 6, t_scale=args.serve_time_scale)
     gen_s = time.time() - t0
     b = api.Batch(device=device(), hbm_budget_bytes=150e9)
     ids = {}
@@ -597,8 +612,9 @@ def run_served_leg(args, fp64_value):
             if fp64_value else None,
             "tuning_s": round(stats["tuning_ms"] / 1e3, 3), "size_buckets_tuned": stats["tunings"],
             "rows_per_item": stats["rows_per_item"], "ctas_per_sm": stats["ctas_per_sm"] or "all",
-            "workload": "served FP32: Poisson arrivals 20/s, side log-uniform 256-4096, durations U(1,6) h x %g, "
-                        "HBM budget 150 GB, continuous admission" % args.serve_time_scale,
+            "workload": "served FP32: Poisson arrivals 20/s, side log-uniform 256-4096, dx 1 m plane + bumps, "
+                        "n 0.03, gamma 5-min hyetograph mean 20 mm/h, durations U(0.5,6) h x %g, HBM budget 150 GB, "
+                        "continuous admission" % args.serve_time_scale,
             "input_generation_s": round(gen_s, 1)}
 
 

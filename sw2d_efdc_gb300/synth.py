@@ -203,5 +203,17 @@ def batch_scenario(side: int, rng, dx: float = 1.0) -> Scenario:
                     t_end=hours * 3600.0)
 
 
+def served_request(side: int, rng, dx: float = 1.0) -> Scenario:
+    """One request of the served form: the precision workload's generator
+    (1 % plane falling to the south edge + Gaussian bumps sigma 0.3 m, corr
+    50 m; n 0.03; gamma 5-min hyetograph, shape 0.8, mean 20 mm/h) on a
+    side x side raster, for a duration U(0.5, 6) h."""
+    z = tilted_plane(side, side, dx, 0.01, 0.3, 50.0, int(rng.integers(1 << 31)))
+    hours = rng.uniform(0.5, 6.0)
+    rain = gamma_hyetograph(int(np.ceil(hours * 12)), 0.8, 20.0, 300.0, rng)
+    return Scenario("served-%d" % side, z, np.zeros_like(z), dx, manning=0.03, rain_mm=rain, dtrain=300.0,
+                    series_mode=2, dt_mode=1, cfl=0.7, dt_max=2.0, outflow_south=True, t_end=hours * 3600.0)
+
+
 def poisson_arrivals(n: int, lam: float, rng) -> np.ndarray:
     return np.cumsum(rng.exponential(1.0 / lam, n))
