@@ -263,6 +263,14 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 3) k64_flux(StepParams p, i
     __shared__ unsigned char regx[SW2D_BY][SW2D_BX], regy[SW2D_BY][SW2D_BX];
     __shared__ double sea[SW2D_BY + 1][SW2D_BX], sec[SW2D_BY + 1][SW2D_BX];
     __shared__ double seb[SW2D_BY][SW2D_BX + 1], sed[SW2D_BY][SW2D_BX + 1];
+    /* the block's momentum faces, packed (thread << 1 | axis), so that the
+     * binary64 momentum update runs on full warps whatever the mix of face
+     * kinds (weir and dry-bed faces sit among momentum faces on steep thin
+     * films); hhb = hb + zb of each momentum face, kept from the
+     * classification */
+    __shared__ unsigned short mlist[2 * SW2D_BX * SW2D_BY];
+    __shared__ double mhhb[2 * SW2D_BX * SW2D_BY];
+    __shared__ int mwarp[SW2D_BX * SW2D_BY / 32 + 1];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int c = blockIdx.x * SW2D_BX + tx;
     const int r = blockIdx.y * SW2D_BY + ty;
@@ -291,6 +299,11 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 3) k64_flux(StepParams p, i
     }
     regx[ty][tx] = (unsigned char)(fx.kind == 1);
     regy[ty][tx] = (unsigned char)(fy.kind == 1);
+    const int t = ty * SW2D_BX + tx, lane = t & 31, warp = t >> 5;
+    if (fx.kind == 1) mhhb[2 * t] = fx.hhb;
+    if (fy.kind == 1) mhhb[2 * t + 1] = fy.hhb;
+    const unsigned bx = __ballot_sync(0xffffffffu, fx.kind == 1), by = __ballot_sync(0xffffffffu, fy.kind == 1);
+    if (lane == 0) mwarp[warp] = __popc(bx) + __popc(by);
     __syncthreads();
     /* 2: each edge once, where a momentum face of the block reads it */
     {
@@ -311,13 +324,22 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 3) k64_flux(StepParams p, i
             sed[tx][0] = regy[tx][0] ? edge_term(vv1[l + 1], vv1[l], vno[l], vno[l + 1]) : 0.0;
         }
     }
+    {
+        int base = 0;
+        for (int w = 0; w < warp; w++) base += mwarp[w];
+        const unsigned lt = (1u << lane) - 1u;
+        const int off = base + __popc(bx & lt) + __popc(by & lt);
+        if (fx.kind == 1) mlist[off] = (unsigned short)(2 * t);
+        if (fy.kind == 1) mlist[off + (fx.kind == 1 ? 1 : 0)] = (unsigned short)(2 * t + 1);
+    }
     __syncthreads();
-    /* 3: face discharges */
+    /* 3: face discharges: the non-momentum faces by their own thread, then
+     * the momentum faces from the packed list */
     bool okx = false, oky = false;
     double hmx = 0, hmy = 0, vx = 0, vy = 0;
     if (in) {
         if (s.active) {
-            const double dt2 = s.dt2, dt2dx = s.dt2dx, dt2dy = s.dt2dy, gg = p.g;
+            const double gg = p.g;
             /* mean depths of the two faces: the momentum update and the CFL speed */
             const double hmX = (doX && r > 0) ? sw2d_half(h[i] + h[i - P]) : 0.0;
             const double hmY = (doY && c > 0) ? sw2d_half(h[i] + h[i - 1]) : 0.0;
@@ -327,27 +349,13 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 3) k64_flux(StepParams p, i
                     const double hw = h[i - P];
                     F = ((p.flags[i - P] & SW2D_F_ACTIVE) && sw2d_gt_pos(hw, th)) ? 0.5440 * hw * sw2d_sqrt_rn(gg * hw)
                                                                                      : 0.0;
-                } else if (fx.kind == 1) {
-                    const double u11 = dt2dx * (sea[ty + 1][tx] - sea[ty][tx]);
-                    const double u12 = (c == 0) ? 0.0 : dt2dy * (seb[ty][tx + 1] - seb[ty][tx]);
-                    const double vt = sw2d_quarter(vv1[i] + vv1[i + 1] + vv1[i - P] + vv1[i - P + 1]);
-                    F = face_momentum(p, fx, hmX, umo[i], uu1[i], vt, u11, u12, dt2, dt2dx, i - P, i);
                 } else {
                     F = face_special(fx, th, gg);
                 }
-                p.qx[1][i] = F;
+                if (fx.kind != 1) p.qx[1][i] = F;
             }
             if (doY) {
-                double F;
-                if (fy.kind == 1) {
-                    const double v11 = (r == 0) ? 0.0 : dt2dx * (sec[ty + 1][tx] - sec[ty][tx]);
-                    const double v12 = dt2dy * (sed[ty][tx + 1] - sed[ty][tx]);
-                    const double ut = sw2d_quarter(uu1[i] + uu1[i + P] + uu1[i - 1] + uu1[i + P - 1]);
-                    F = face_momentum(p, fy, hmY, vno[i], vv1[i], ut, v11, v12, dt2, dt2dy, i - 1, i);
-                } else {
-                    F = face_special(fy, th, gg);
-                }
-                p.qy[1][i] = F;
+                if (fy.kind != 1) p.qy[1][i] = face_special(fy, th, gg);
             }
             if (p.dt_mode == 1) {
                 const uint8_t fc = p.flags[i];
@@ -361,6 +369,38 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 3) k64_flux(StepParams p, i
                     oky = sw2d_ge_pos(hmy, th);
                     vy = vv1[i];
                 }
+            }
+        }
+    }
+    /* the momentum faces, packed: face k of the list is a face of cell
+     * (ry, rx) of the block, x (north) or y (west) by its low bit */
+    if (s.active) {
+        int M = 0;
+        for (int w = 0; w < SW2D_BX * SW2D_BY / 32; w++) M += mwarp[w];
+        const double dt2 = s.dt2, dt2dx = s.dt2dx, dt2dy = s.dt2dy;
+        for (int k = t; k < M; k += SW2D_BX * SW2D_BY) {
+            const int id = mlist[k], ft = id >> 1, lx = ft % SW2D_BX, ly = ft / SW2D_BX;
+            const int cc = blockIdx.x * SW2D_BX + lx, rr = blockIdx.y * SW2D_BY + ly;
+            const size_t j = (size_t)(rr + H) * P + (cc + H);
+            FaceK f;
+            f.kind = 1;
+            f.hhb = mhhb[id];
+            if ((id & 1) == 0) { /* x face north of cell j */
+                f.ha = h[j - P];
+                f.za = p.z[j - P];
+                const double hm = sw2d_half(h[j] + h[j - P]);
+                const double u11 = dt2dx * (sea[ly + 1][lx] - sea[ly][lx]);
+                const double u12 = (cc == 0) ? 0.0 : dt2dy * (seb[ly][lx + 1] - seb[ly][lx]);
+                const double vt = sw2d_quarter(vv1[j] + vv1[j + 1] + vv1[j - P] + vv1[j - P + 1]);
+                p.qx[1][j] = face_momentum(p, f, hm, umo[j], uu1[j], vt, u11, u12, dt2, dt2dx, j - P, j);
+            } else { /* y face west of cell j */
+                f.ha = h[j - 1];
+                f.za = p.z[j - 1];
+                const double hm = sw2d_half(h[j] + h[j - 1]);
+                const double v11 = (rr == 0) ? 0.0 : dt2dx * (sec[ly + 1][lx] - sec[ly][lx]);
+                const double v12 = dt2dy * (sed[ly][lx + 1] - sed[ly][lx]);
+                const double ut = sw2d_quarter(uu1[j] + uu1[j + P] + uu1[j - 1] + uu1[j + P - 1]);
+                p.qy[1][j] = face_momentum(p, f, hm, vno[j], vv1[j], ut, v11, v12, dt2, dt2dy, j - 1, j);
             }
         }
     }
