@@ -229,7 +229,6 @@ __device__ __forceinline__ double face_momentum(const StepParams& p, const FaceK
 }
 
 __device__ unsigned long long block_max_u64(unsigned long long v, unsigned long long* sm);
-__device__ float block_max_f32_all(float v, float* sm);
 
 /* CFL speed contribution of one face of the entering state: (|velocity| +
  * sqrt(g * mean depth)) / spacing for faces between two active cells whose
@@ -238,26 +237,77 @@ __device__ __forceinline__ double face_speed(double vel, double hm, double g, do
     return (fabs(vel) + sw2d_sqrt_rn(g * hm)) * rd;
 }
 
-/* exact block maximum of face speeds: binary32 estimate for every face,
- * binary64 only for the faces within 1e-5 of the block's binary32 maximum */
-__device__ __forceinline__ unsigned long long block_face_speed_max(bool ok, double vel, double hm, double g,
-                                                                   double rd, float* smf,
-                                                                   unsigned long long* smu) {
-    /* binary32 estimates by integer operations: a conversion from binary64
-     * costs a binary64 operation on this GPU */
-    const float s32 = ok ? (fabsf(sw2d_f32_est_of_f64(vel)) +
-                            sqrtf(sw2d_f32_est_of_f64(g) * sw2d_f32_est_of_f64(hm))) *
-                               sw2d_f32_est_of_f64(rd)
-                         : 0.0f;
-    const float m32 = block_max_f32_all(s32, smf);
-    unsigned long long bits = 0ull;
-    if (ok && s32 >= m32 * 0.99999f) bits = (unsigned long long)__double_as_longlong(face_speed(vel, hm, g, rd));
-    return block_max_u64(bits, smu);
+#define NWARP (SW2D_BX * SW2D_BY / 32)
+
+__device__ __forceinline__ int tid_linear() { return threadIdx.y * SW2D_BX + threadIdx.x; }
+
+/* binary32 estimate of a face speed, from integer operations: a conversion
+ * from binary64 costs a binary64 operation on this GPU */
+__device__ __forceinline__ float face_speed_est(bool ok, double vel, double hm, double g, double rd) {
+    return ok ? (fabsf(sw2d_f32_est_of_f64(vel)) + sqrtf(sw2d_f32_est_of_f64(g) * sw2d_f32_est_of_f64(hm))) *
+                    sw2d_f32_est_of_f64(rd)
+              : 0.0f;
+}
+
+/* exact block maxima of the x and the y face speeds together: binary32
+ * estimates for every face, binary64 only for the faces within 1e-5 of the
+ * block's binary32 maximum; both reductions share their barriers.  The
+ * maxima are valid in thread 0. */
+__device__ __forceinline__ void block_face_speed_max2(bool okx, double vx, double hmx, double rdx, bool oky,
+                                                      double vy, double hmy, double rdy, double g, float* smf,
+                                                      unsigned long long* smu, unsigned long long* sx,
+                                                      unsigned long long* sy) {
+    const int lane = tid_linear() & 31, warp = tid_linear() >> 5;
+    const float ex = face_speed_est(okx, vx, hmx, g, rdx), ey = face_speed_est(oky, vy, hmy, g, rdy);
+    float mx = ex, my = ey;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, o));
+    }
+    if (lane == 0) {
+        smf[warp] = mx;
+        smf[NWARP + warp] = my;
+    }
+    __syncthreads();
+    mx = smf[0];
+    my = smf[NWARP];
+#pragma unroll
+    for (int k = 1; k < NWARP; k++) {
+        mx = fmaxf(mx, smf[k]);
+        my = fmaxf(my, smf[NWARP + k]);
+    }
+    unsigned long long bx = 0ull, by = 0ull;
+    if (okx && ex >= mx * 0.99999f) bx = (unsigned long long)__double_as_longlong(face_speed(vx, hmx, g, rdx));
+    if (oky && ey >= my * 0.99999f) by = (unsigned long long)__double_as_longlong(face_speed(vy, hmy, g, rdy));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ux = __shfl_down_sync(0xffffffffu, bx, o), uy = __shfl_down_sync(0xffffffffu, by, o);
+        bx = ux > bx ? ux : bx;
+        by = uy > by ? uy : by;
+    }
+    if (lane == 0) {
+        smu[warp] = bx;
+        smu[NWARP + warp] = by;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        bx = lane < NWARP ? smu[lane] : 0ull;
+        by = lane < NWARP ? smu[NWARP + lane] : 0ull;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ux = __shfl_down_sync(0xffffffffu, bx, o), uy = __shfl_down_sync(0xffffffffu, by, o);
+            bx = ux > bx ? ux : bx;
+            by = uy > by ? uy : by;
+        }
+    }
+    *sx = bx;
+    *sy = by;
 }
 
 __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 3) k64_flux(StepParams p, int cur) {
-    __shared__ float smf[SW2D_BX * SW2D_BY / 32];
-    __shared__ unsigned long long smu[SW2D_BX * SW2D_BY / 32];
+    __shared__ float smf[2 * SW2D_BX * SW2D_BY / 32];
+    __shared__ unsigned long long smu[2 * SW2D_BX * SW2D_BY / 32];
     /* momentum faces of the block, then the edges of the block's cells and of
      * the row above / column left of it */
     __shared__ unsigned char regx[SW2D_BY][SW2D_BX], regy[SW2D_BY][SW2D_BX];
@@ -405,8 +455,8 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY, 3) k64_flux(StepParams p, i
         }
     }
     if (p.dt_mode == 1) {
-        const unsigned long long sx = block_face_speed_max(okx, vx, hmx, p.g, p.rdx, smf, smu);
-        const unsigned long long sy = block_face_speed_max(oky, vy, hmy, p.g, p.rdy, smf, smu);
+        unsigned long long sx, sy;
+        block_face_speed_max2(okx, vx, hmx, p.rdx, oky, vy, hmy, p.rdy, p.g, smf, smu, &sx, &sy);
         if (threadIdx.x == 0 && threadIdx.y == 0) {
             const int b = blockIdx.y * gridDim.x + blockIdx.x;
             p.partials_f[2 * b] = __longlong_as_double((long long)sx);
@@ -453,9 +503,6 @@ __device__ __forceinline__ double continuity(const StepParams& p, size_t i, uint
 /* ------------------------------------------------------------------------ */
 /* block reductions (fixed order: deterministic for a given grid)            */
 
-#define NWARP (SW2D_BX * SW2D_BY / 32)
-
-__device__ __forceinline__ int tid_linear() { return threadIdx.y * SW2D_BX + threadIdx.x; }
 
 __device__ __forceinline__ double block_sum(double v, double* sm) {
     const int lane = tid_linear() & 31, warp = tid_linear() >> 5;
@@ -493,19 +540,6 @@ __device__ unsigned long long block_max_u64(unsigned long long v, unsigned long 
         }
     }
     return t; /* valid in thread 0 */
-}
-
-__device__ float block_max_f32_all(float v, float* sm) {
-    const int lane = tid_linear() & 31, warp = tid_linear() >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-    __syncthreads();
-    if (lane == 0) sm[warp] = v;
-    __syncthreads();
-    float t = sm[0];
-#pragma unroll
-    for (int k = 1; k < NWARP; k++) t = fmaxf(t, sm[k]);
-    return t; /* valid in every thread */
 }
 
 #define NPART 4 /* rain, evap, qout, s_max bits */
@@ -733,8 +767,8 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_update(StepParams p, in
  * prepares the next slot. */
 __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int cur, int full) {
     __shared__ double smd[NWARP];
-    __shared__ float smf[NWARP];
-    __shared__ unsigned long long smu[NWARP];
+    __shared__ float smf[2 * NWARP];
+    __shared__ unsigned long long smu[2 * NWARP];
     __shared__ bool last;
     const int c = blockIdx.x * SW2D_BX + threadIdx.x;
     const int r = blockIdx.y * SW2D_BY + threadIdx.y;
@@ -761,8 +795,8 @@ __global__ void __launch_bounds__(SW2D_BX * SW2D_BY) k64_prime(StepParams p, int
         }
     }
     vol = block_sum(vol, smd);
-    const unsigned long long sx = block_face_speed_max(okx, vx, hmx, p.g, p.rdx, smf, smu);
-    const unsigned long long sy = block_face_speed_max(oky, vy, hmy, p.g, p.rdy, smf, smu);
+    unsigned long long sx, sy;
+    block_face_speed_max2(okx, vx, hmx, p.rdx, oky, vy, hmy, p.rdy, p.g, smf, smu, &sx, &sy);
     const int tid = tid_linear();
     const int b = blockIdx.y * gridDim.x + blockIdx.x;
     if (tid == 0) {
