@@ -1,6 +1,8 @@
-/* Host engine of the FP32 precision form: owns the scenarios that one fused
- * kernel launch advances together (one scenario for a single raster, many
- * for the batched and served forms). */
+/* Host engine of the FP32 precision form: owns the scenarios that one
+ * persistent launch per feature class advances together, a chunk of
+ * iterations at a time (one scenario for a single raster, many for the
+ * batched and served forms), and the autotuner that chooses the work split
+ * (rows per work item, CTAs per SM) per size bucket. */
 #ifndef SW2D_ENGINE_H
 #define SW2D_ENGINE_H
 

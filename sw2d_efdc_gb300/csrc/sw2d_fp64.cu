@@ -5,8 +5,10 @@
  * FP64 instructions, not HBM.  The step is therefore split so that nothing
  * FP64 is computed twice, in two kernels per iteration:
  *   k64_flux   : new x/y face discharges of every face (flux, :97-353) from the
- *                stored face velocities uu1/vv1 of the previous iteration,
- *                and the CFL face-speed maxima of the entering state
+ *                stored face velocities uu1/vv1 of the previous iteration
+ *                (the block's momentum faces packed into a list so that
+ *                their binary64 update runs on full warps), and the CFL
+ *                face-speed maxima of the entering state
  *   k64_update : per tile, the provisional depth (continuity at t,
  *                :602-664) -> "active and h* < th" flags in shared memory;
  *                treat_error (:695-725, restated per face) and the final
