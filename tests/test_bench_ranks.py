@@ -144,3 +144,22 @@ def test_fp32_only_cells_counts_leave_one_out():
     assert p["p3"]["fp32_worst_unexplained_m"] == 0.005
     loo = out["leave_one_out"]
     assert loo["perturbed_runs_max"] == 1 and loo["perturbed_worst_m_max"] == 0.004
+
+
+def test_benchmark_workloads_follow_their_configs():
+    """The batched and served legs' synthetic inputs have the shapes the
+    workloads name: batched, sides log-uniform in [128, 2048] with a
+    three-class Manning raster and 1-6 h of rain; served, sides in
+    [256, 4096] with the precision workload's generator (uniform n 0.03,
+    5-min gamma hyetograph) and 0.5-6 h durations, scaled as asked."""
+    import bench
+    b = bench.make_batch_specs(12, 128, 2048, 4)
+    assert all(128 <= s["dem"].shape[0] == s["dem"].shape[1] <= 2048 for s in b)
+    assert all(set(np.unique(s["manning_classes"])) <= {0, 1, 2} for s in b)
+    assert all(len(s["manning_table"]) == 3 and 3600.0 <= s["t_end"] <= 6 * 3600.0 for s in b)
+    v = bench.make_served_specs(6, 6, t_scale=0.25)
+    assert all(256 <= s["dem"].shape[0] == s["dem"].shape[1] <= 4096 for s in v)
+    assert all(s["manning"] == 0.03 and "manning_classes" not in s for s in v)
+    assert all(s["dtrain"] == 300.0 and 0.5 * 3600 * 0.25 <= s["t_end"] <= 6 * 3600 * 0.25 for s in v)
+    # the plane falls towards the south edge (row 0 is the north row)
+    assert all(s["dem"][0].mean() > s["dem"][-1].mean() for s in v)
